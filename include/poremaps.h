@@ -1,0 +1,191 @@
+/*
+ * poremaps_gb300 -- C ABI of the GB300 (sm_103a) POREMAPS permeability solver.
+ *
+ * One process, one GPU, one device-resident domain per problem.  Every entry
+ * point is extern "C", takes plain pointers and sizes, returns pm_status and
+ * never aborts or prints.  The library owns all device memory it allocates;
+ * host buffers passed in are owned by the caller.  Calls on distinct problems
+ * are thread-safe (each problem has its own CUDA stream); calls on one
+ * problem must not overlap.
+ *
+ * Reference interfaces replaced (paths inside the krachdd/poremaps project):
+ *   pm_read_params        read_problem_params / read_parallel_params
+ *                         (src/read_problem_params.cc:50-156)
+ *   pm_read_geometry      read_geometry (src/geometry.cc:58-126)
+ *   pm_problem_create     get_dom_limits + eval_geometry + allocate_initial_field
+ *                         + set_halos_initial (src/geometry.cc:129-302,
+ *                         src/initialize.cc:69-289, src/main_stokes_solver.cc:161-276)
+ *   pm_solve              calc_flow (src/calc_flow.cc:53-169; declared in
+ *                         src/calc_flow.h:36-61)
+ *   pm_iterate            one calc_flow iteration body: central_diff5
+ *                         (src/solver.cc:112-224) + communicate_halos
+ *                         (src/parallelization.cc:193-318) +
+ *                         reapply_pressure_gradient (src/boundary_conditions.cc:46-79)
+ *   pm_compute_convergence compute_convergence (src/evaluation.cc:216-262)
+ *   pm_compute_permeability compute_permeability (src/evaluation.cc:54-211)
+ *   pm_get_porosity       get_porosity (src/geometry.cc:335-364)
+ *   pm_get_fields / pm_write_outputs / pm_write_log_row
+ *                         write_output_raw, write_domain_decomposition,
+ *                         write_logfile (src/output.cc:53-230)
+ *   pm_run_inp            the POREMAPS program (src/main_stokes_solver.cc:57-416)
+ */
+#ifndef POREMAPS_GB300_H
+#define POREMAPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PM_OK = 0,
+  PM_ERR_INVALID = 1,   /* bad argument or parameter value */
+  PM_ERR_IO = 2,        /* file missing, short or unwritable */
+  PM_ERR_CUDA = 3,      /* CUDA runtime error (message in pm_last_error) */
+  PM_ERR_NOMEM = 4,     /* device or host allocation failed / over budget */
+  PM_ERR_NONFINITE = 5, /* NaN/Inf detected in a reduction */
+  PM_ERR_BUSY = 6,      /* server full / request not finished */
+  PM_ERR_NOT_FOUND = 7
+} pm_status;
+
+/* sweep ordering on the device */
+typedef enum {
+  PM_ORDER_DEFAULT = -1,  /* REDBLACK for every solver */
+  PM_ORDER_REFERENCE = 0, /* the reference's in-place lexicographic order, run as an exact
+                             hyperplane wavefront: bit-identical to the reference */
+  PM_ORDER_JACOBI = 1,    /* ping-pong: every neighbour from the previous iterate
+                             (diverges for solver 1, whose pressure update uses the
+                             pre-update velocities; solvers 2 and 3 are stable) */
+  PM_ORDER_REDBLACK = 2   /* red then black half-sweeps, +-2 same-colour reads old */
+} pm_order;
+
+typedef enum {
+  PM_PREC_FP64 = 0,  /* fields stored and swept in FP64 */
+  PM_PREC_MIXED = 1  /* FP32 correction sweeps + FP64 residual/defect correction
+                        (Jacobi ordering; solvers 2 and 3) */
+} pm_precision;
+
+typedef enum {
+  PM_ARITH_EXACT = 0, /* the reference's operation order, no FMA contraction */
+  PM_ARITH_FAST = 1   /* coefficient form with FMA (a few ulp from EXACT per sweep) */
+} pm_arith;
+
+/* The 14 keys of the reference .inp file (input_template.inp, README.md:86-101), in order,
+ * plus GPU extensions. */
+typedef struct {
+  int dom_decomposition[3];     /* parsed and ignored: one device-resident domain */
+  int boundary_method;          /* 0..4 */
+  char geometry_file_name[400];
+  int size[3];                  /* nx, ny, nz */
+  double voxel_size;            /* m */
+  int max_iter;
+  int it_eval;
+  int it_write;
+  char log_file_name[400];
+  unsigned solving_algorithm;   /* 1 Jacobi, 2 Gauss-Seidel, 3 SOR (update formula) */
+  double eps;
+  double porosity;              /* -1: computed from the geometry */
+  int dom_interest[6];          /* xmin xmax ymin ymax zmin zmax (inclusive), all 0 = off */
+  int write_output[4];          /* vel, press, neighbourhood, domain decomposition */
+  /* ---- GPU extensions (pm_params_default sets them) ---- */
+  int order;                    /* pm_order */
+  int precision;                /* pm_precision */
+  int arith;                    /* pm_arith (FP64 sweeps) */
+  int write_log;                /* 1: append the reference log rows to log_file_name */
+  int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
+} pm_params;
+
+typedef struct {
+  int iterations;     /* iteration index of the last convergence evaluation */
+  int sweeps;         /* sweeps performed (iterations + 1 when stopped by eps) */
+  int converged;      /* 1 if conv < eps stopped the loop */
+  double conv;
+  double permeability; /* mean(w)/Re in voxel units (compute_convergence) */
+  double k13, k23, k33;        /* dom_interest box (0 if off) */
+  double wk13, wk23, wk33;     /* whole domain, m^2 */
+  double wmax_velz, wmean_velz; /* m/s (velocity x voxel size) */
+  double porosity;
+  double device_ms;   /* device time of the sweep loop (CUDA events on the problem stream) */
+  double wall_ms;     /* host wall time of pm_solve */
+  double glups;       /* nx*ny*nz*sweeps / device time, 1e9/s */
+} pm_result;
+
+typedef struct pm_problem pm_problem;
+
+const char* pm_last_error(void);
+const char* pm_version(void);
+pm_status pm_params_default(pm_params* p);
+
+pm_status pm_read_params(const char* inp_path, pm_params* out);
+pm_status pm_read_geometry(const char* raw_path, const int size[3], uint8_t* out);
+
+/* geom: nx*ny*nz bytes, x fastest, 0 = fluid, nonzero = solid (copied to the device). */
+pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem** out);
+pm_status pm_problem_destroy(pm_problem* pr);
+
+/* Full calc_flow loop; fills res.  Re-entrant: a second call continues iterating. */
+pm_status pm_solve(pm_problem* pr, pm_result* res);
+/* n iterations (sweep + halo exchange + pressure reapply) without convergence checks. */
+pm_status pm_iterate(pm_problem* pr, int n);
+pm_status pm_compute_convergence(pm_problem* pr, double* permeability, double* conv);
+pm_status pm_compute_permeability(pm_problem* pr, pm_result* res);
+pm_status pm_get_porosity(pm_problem* pr, double* porosity);
+pm_status pm_get_iteration(pm_problem* pr, int* iteration);
+
+/* Interior fields, x fastest, nx*ny*nz doubles each; any pointer may be NULL.
+ * Unscaled (the writers multiply velocities by voxel_size). */
+pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double* p);
+/* Interior neighbourhood codes 100*cx + 10*cy + cz (-1 solid), x fastest. */
+pm_status pm_get_neighborhood(pm_problem* pr, int32_t* out);
+/* Writes velx_/vely_/velz_/press_/voxel_neighborhood_/domain_decomp_ + geometry name per
+ * write_output, byte-compatible with the reference writers. */
+pm_status pm_write_outputs(pm_problem* pr);
+
+/* The whole POREMAPS program on one .inp file (log + field files); res may be NULL. */
+pm_status pm_run_inp(const char* inp_path, const pm_params* overrides, pm_result* res);
+
+/* Full permeability tensor from three axis-rotated solves of one geometry
+ * (README.md:215-227).  K is row-major 3x3 in m^2, K[3*i+j] = k_(i+1)(j+1): the
+ * response along axis i to a unit pressure drop along axis j.  res3 (may be NULL)
+ * receives the three solves (flow along x, y, z). */
+pm_status pm_solve_tensor(const pm_params* p, const uint8_t* geom, double K[9],
+                          pm_result res3[3]);
+
+/* ---- batched / serving form: many uneven samples resident at once ---- */
+typedef struct {
+  size_t hbm_budget_bytes;  /* admission budget for resident problems (0 = 80% of free) */
+  int max_resident;         /* slot limit (0 = 1024) */
+  int precision;            /* pm_precision for all requests */
+  int use_graphs;           /* capture each it_eval block of sweeps in a CUDA graph */
+  int autotune;             /* pick tile shapes per size class by timing */
+} pm_server_config;
+
+typedef struct pm_server pm_server;
+
+typedef struct {
+  uint64_t ticket;
+  pm_status status;
+  pm_result result;
+  double submit_ms, admit_ms, finish_ms; /* server clock */
+} pm_completion;
+
+pm_status pm_server_create(const pm_server_config* cfg, pm_server** out);
+pm_status pm_server_destroy(pm_server* s);
+/* Queue one request (geometry copied).  Never blocks. */
+pm_status pm_server_submit(pm_server* s, const pm_params* p, const uint8_t* geom,
+                           uint64_t* ticket);
+/* Advance the device by one scheduling round (admit, one it_eval block for every
+ * resident request, retire converged ones).  *active = resident + queued after the round. */
+pm_status pm_server_step(pm_server* s, int* active);
+/* Move up to max finished requests into out; *n = number written. */
+pm_status pm_server_poll(pm_server* s, pm_completion* out, int max, int* n);
+pm_status pm_server_stats(pm_server* s, double* busy_ms, double* wall_ms, uint64_t* lups);
+double pm_server_clock_ms(pm_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,637 @@
+/*
+ * CPU ORACLE for the POREMAPS pseudo-time Stokes sweep -- TEST INFRASTRUCTURE.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+ * this file, as the checker.  The poremaps_gb300 product never links it.
+ *
+ * Each function restates one reference routine (file:line in the reference
+ * project krachdd/poremaps) in single-process C.  The "ranks" of the
+ * reference become z-slabs of one process (the reference run with
+ * dom_decomposition 1 1 P), which lets the CPU baseline use P host cores with
+ * the reference's own per-rank semantics; nslabs = 1 is the single-rank run.
+ *
+ * Floating-point expressions keep the reference's operand order and are built
+ * with -ffp-contract=off, so results are bitwise identical to the reference
+ * binary (pinned by tests/test_oracle_golden.py).
+ */
+#define _POSIX_C_SOURCE 200809L
+#include "pm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* constants.h:46-64 */
+#define OMEGA_SOR 1.2
+#define RE 0.01
+#define C2 1.5e6
+#define DT 1.0e-4
+#define LIM 2
+
+typedef struct {
+  int NX, NY, NZ; /* padded sizes of this slab */
+  int lnz, z0;    /* interior z extent and global z start */
+  unsigned char* g;
+  int* nh;
+  double *u, *v, *w, *p;
+  double *u2, *v2, *w2, *p2;
+  double* p3; /* swept (pre-reapply) pressure of the last interior plane */
+} slab;
+
+struct or_problem {
+  int nx, ny, nz;
+  int bc;
+  unsigned solver;
+  int ns;
+  int periods[3];
+  double dx, porosity_in, phi;
+  int di[6];
+  slab* s;
+  int iteration;
+  int nthreads;
+};
+
+static inline long IDX(const slab* S, int z, int y, int x) {
+  return ((long)z * S->NY + y) * S->NX + x;
+}
+
+/* ---------------------------------------------------------------------- */
+/* halo exchange: parallelization.cc:67-190 (geometry) and :193-318 (fields).
+ * X then Y then Z, 2-deep faces over the full extent of the other axes.  In
+ * x and y the only neighbour is the slab itself (periodic) or none; in z the
+ * neighbours are the adjacent slabs (wrapping when periodic). */
+#define DEF_EXCHANGE(NAME, T)                                                          \
+  static void NAME(or_problem* pr, T** arr) {                                          \
+    for (int c = 0; c < pr->ns; ++c) {                                                 \
+      slab* S = &pr->s[c];                                                             \
+      T* a = arr[c];                                                                   \
+      int nx = S->NX, ny = S->NY, nz = S->NZ;                                          \
+      if (pr->periods[0])                                                              \
+        for (int i = 0; i < nz; i++)                                                   \
+          for (int j = 0; j < ny; j++) {                                               \
+            T s2 = a[IDX(S, i, j, 2)], s3 = a[IDX(S, i, j, 3)];                        \
+            T r0 = a[IDX(S, i, j, nx - 4)], r1 = a[IDX(S, i, j, nx - 3)];              \
+            a[IDX(S, i, j, nx - 2)] = s2; a[IDX(S, i, j, nx - 1)] = s3;                 \
+            a[IDX(S, i, j, 0)] = r0; a[IDX(S, i, j, 1)] = r1;                           \
+          }                                                                            \
+      if (pr->periods[1])                                                              \
+        for (int i = 0; i < nz; i++)                                                   \
+          for (int k = 0; k < nx; k++) {                                               \
+            T s2 = a[IDX(S, i, 2, k)], s3 = a[IDX(S, i, 3, k)];                        \
+            T r0 = a[IDX(S, i, ny - 4, k)], r1 = a[IDX(S, i, ny - 3, k)];              \
+            a[IDX(S, i, ny - 2, k)] = s2; a[IDX(S, i, ny - 1, k)] = s3;                 \
+            a[IDX(S, i, 0, k)] = r0; a[IDX(S, i, 1, k)] = r1;                           \
+          }                                                                            \
+    }                                                                                  \
+    /* z: pack every slab's send planes first (MPI_Sendrecv semantics) */              \
+    int ns = pr->ns;                                                                   \
+    T** lo = (T**)malloc(sizeof(T*) * ns);                                             \
+    T** hi = (T**)malloc(sizeof(T*) * ns);                                             \
+    for (int c = 0; c < ns; ++c) {                                                     \
+      slab* S = &pr->s[c];                                                             \
+      long plane = (long)S->NX * S->NY;                                                \
+      lo[c] = (T*)malloc(sizeof(T) * 2 * plane);                                       \
+      hi[c] = (T*)malloc(sizeof(T) * 2 * plane);                                       \
+      memcpy(lo[c], arr[c] + 2 * plane, sizeof(T) * 2 * plane);                        \
+      memcpy(hi[c], arr[c] + (long)(S->NZ - 4) * plane, sizeof(T) * 2 * plane);         \
+    }                                                                                  \
+    for (int c = 0; c < ns; ++c) {                                                     \
+      slab* S = &pr->s[c];                                                             \
+      long plane = (long)S->NX * S->NY;                                                \
+      int up = c + 1, dn = c - 1;                                                      \
+      if (up == ns) up = pr->periods[2] ? 0 : -1;                                       \
+      if (dn < 0) dn = pr->periods[2] ? ns - 1 : -1;                                    \
+      if (up >= 0) memcpy(arr[c] + (long)(S->NZ - 2) * plane, lo[up], sizeof(T) * 2 * plane); \
+      if (dn >= 0) memcpy(arr[c], hi[dn], sizeof(T) * 2 * plane);                       \
+    }                                                                                  \
+    for (int c = 0; c < ns; ++c) { free(lo[c]); free(hi[c]); }                         \
+    free(lo); free(hi);                                                                \
+  }
+
+DEF_EXCHANGE(exchange_u8, unsigned char)
+DEF_EXCHANGE(exchange_f64, double)
+
+static void exchange_field(or_problem* pr, int which) {
+  double** arr = (double**)malloc(sizeof(double*) * pr->ns);
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    arr[c] = which == 0 ? S->p : which == 1 ? S->u : which == 2 ? S->v : S->w;
+  }
+  exchange_f64(pr, arr);
+  free(arr);
+}
+
+/* ---------------------------------------------------------------------- */
+/* eval_geometry: geometry.cc:174-302 (Bentz et al. 2007 neighbourhood). */
+static void eval_geometry(slab* S) {
+  long n = (long)S->NX * S->NY * S->NZ;
+  for (long c = 0; c < n; ++c) S->nh[c] = S->g[c] == 0 ? 0 : -1;
+  const long st[3] = {1, S->NX, (long)S->NX * S->NY};
+  const int shift[3] = {100, 10, 1};
+  for (int d = 0; d < 3; ++d)
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++) {
+          long c = IDX(S, i, j, k);
+          if (S->g[c] != 0) continue;
+          int l = S->g[c - st[d]] != 0, r = S->g[c + st[d]] != 0;
+          int ll = -1, rr = -1;
+          if (!l) ll = S->g[c - 2 * st[d]] != 0;
+          if (!r) rr = S->g[c + 2 * st[d]] != 0;
+          int cs = 0;
+          if (l == 1 && r == 1) cs = 1;
+          else if (l == 1 && r == 0 && rr == 1) cs = 2;
+          else if (ll == 1 && l == 0 && r == 1) cs = 3;
+          else if (l == 1 && r == 0 && rr == 0) cs = 4;
+          else if (ll == 0 && l == 0 && r == 1) cs = 5;
+          else if (l == 0 && r == 0) cs = 6;
+          S->nh[c] += cs * shift[d];
+        }
+}
+
+/* ---------------------------------------------------------------------- */
+/* reapply_pressure_gradient: boundary_conditions.cc:46-79 */
+static void reapply(or_problem* pr) {
+  slab* S = &pr->s[0];
+  for (int j = LIM; j < S->NY - LIM; j++)
+    for (int k = LIM; k < S->NX - LIM; k++)
+      if (S->g[IDX(S, 1, j, k)] == 0) S->p[IDX(S, 1, j, k)] = pr->nz + 2;
+  S = &pr->s[pr->ns - 1];
+  for (int j = LIM; j < S->NY - LIM; j++)
+    for (int k = LIM; k < S->NX - LIM; k++) {
+      if (S->g[IDX(S, S->NZ - 2, j, k)] == 0) S->p[IDX(S, S->NZ - 2, j, k)] = 2.0;
+      if (S->g[IDX(S, S->NZ - 3, j, k)] == 0) S->p[IDX(S, S->NZ - 3, j, k)] = 3.0;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* get_2nd_derivation: solver.cc:57-91 (six wall-aware 1-D stencils). */
+static inline double d2(int cs, double ll, double l, double m, double r, double rr) {
+  switch (cs) {
+    case 1: return -8.0 * m;
+    case 2: return 8.0 / 3.0 * r - 16.0 / 3.0 * m;
+    case 3: return 8.0 / 3.0 * l - 16.0 / 3.0 * m;
+    case 4: return 2.0 * r - 5.0 * m - 1.0 / 5.0 * rr;
+    case 5: return 2.0 * l - 1.0 / 5.0 * ll - 5.0 * m;
+    case 6: return l - 2.0 * m + r;
+  }
+  return 0.0;
+}
+
+/* One fluid voxel of central_diff5 (solver.cc:136-220).  Reads the source
+ * arrays s*, writes the destination d*.  In-place (reference order): s == d.
+ * Ping-pong Jacobi: s = old state.  Red-black: see sweep_redblack. */
+static inline void voxel(const slab* S, long c, unsigned solver, const double* su,
+                         const double* sv, const double* sw, const double* sp, double* du,
+                         double* dv, double* dw, double* dpr, const double* p3) {
+  const long sx = 1, sy = S->NX, sz = (long)S->NX * S->NY;
+  const unsigned char* g = S->g;
+  double pxm = sp[c - sx], pym = sp[c - sy];
+  if (p3) {
+    /* Voxel on the last interior plane: in the reference's in-place order its
+     * -x / -y neighbours on the same plane were already swept in this
+     * iteration and hold their pre-reapply pressure (the reapply to 3 runs
+     * after the sweep), so an out-of-place ordering reads the swept values. */
+    long q = c % sz;
+    int k = (int)(q % S->NX), j = (int)(q / S->NX);
+    if (k - 1 >= LIM) pxm = p3[q - sx];
+    if (j - 1 >= LIM) pym = p3[q - sy];
+  }
+  double dp_dz = g[c - sz] == 0 ? -sp[c - sz] + sp[c] : 0.;
+  double dp_dy = g[c - sy] == 0 ? -pym + sp[c] : 0.;
+  double dp_dx = g[c - sx] == 0 ? -pxm + sp[c] : 0.;
+  int code = S->nh[c];
+  int cz = code % 10; code /= 10;
+  int cy = code % 10; code /= 10;
+  int cx = code % 10;
+  double uxx = (su[c - sx] - 2 * su[c] + su[c + sx]);
+  double vyy = (sv[c - sy] - 2 * sv[c] + sv[c + sy]);
+  double wzz = (sw[c - sz] - 2 * sw[c] + sw[c + sz]);
+  double vxx = d2(cx, sv[c - 2 * sx], sv[c - sx], sv[c], sv[c + sx], sv[c + 2 * sx]);
+  double wxx = d2(cx, sw[c - 2 * sx], sw[c - sx], sw[c], sw[c + sx], sw[c + 2 * sx]);
+  double uyy = d2(cy, su[c - 2 * sy], su[c - sy], su[c], su[c + sy], su[c + 2 * sy]);
+  double wyy = d2(cy, sw[c - 2 * sy], sw[c - sy], sw[c], sw[c + sy], sw[c + 2 * sy]);
+  double uzz = d2(cz, su[c - 2 * sz], su[c - sz], su[c], su[c + sz], su[c + 2 * sz]);
+  double vzz = d2(cz, sv[c - 2 * sz], sv[c - sz], sv[c], sv[c + sz], sv[c + 2 * sz]);
+  double fu = uxx + uyy + uzz;
+  double fv = vyy + vzz + vxx;
+  double fw = wzz + wxx + wyy;
+  double v_sum = 0.0;
+  double un = su[c], vn = sv[c], wn = sw[c];
+  if (solver == 1)
+    v_sum = (sw[c + sz] - sw[c] + sv[c + sy] - sv[c] + su[c + sx] - su[c]);
+  if (solver == 1 || solver == 2) {
+    un = g[c - sx] != 0 ? 0.0 : su[c] + (-dp_dx + fu / RE) * DT;
+    vn = g[c - sy] != 0 ? 0.0 : sv[c] + (-dp_dy + fv / RE) * DT;
+    wn = g[c - sz] != 0 ? 0.0 : sw[c] + (-dp_dz + fw / RE) * DT;
+  } else if (solver == 3) {
+    un = (1.0 - OMEGA_SOR) * su[c] + OMEGA_SOR * (-dp_dx + fu / RE) * DT;
+    vn = (1.0 - OMEGA_SOR) * sv[c] + OMEGA_SOR * (-dp_dy + fv / RE) * DT;
+    wn = (1.0 - OMEGA_SOR) * sw[c] + OMEGA_SOR * (-dp_dz + fw / RE) * DT;
+  }
+  if (solver == 2 || solver == 3)
+    v_sum = (sw[c + sz] - wn + sv[c + sy] - vn + su[c + sx] - un);
+  du[c] = un;
+  dv[c] = vn;
+  dw[c] = wn;
+  dpr[c] = sp[c] - C2 * v_sum * DT;
+}
+
+/* central_diff5 (solver.cc:112-224): in-place lexicographic sweep. */
+static void sweep_reference(or_problem* pr, slab* S) {
+  for (int i = LIM; i < S->NZ - LIM; i++)
+    for (int j = LIM; j < S->NY - LIM; j++)
+      for (int k = LIM; k < S->NX - LIM; k++) {
+        long c = IDX(S, i, j, k);
+        if (S->g[c] == 0)
+          voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u, S->v, S->w, S->p, NULL);
+      }
+}
+
+static void swap_state(slab* S) {
+  double* t;
+  t = S->u; S->u = S->u2; S->u2 = t;
+  t = S->v; S->v = S->v2; S->v2 = t;
+  t = S->w; S->w = S->w2; S->w2 = t;
+  t = S->p; S->p = S->p2; S->p2 = t;
+}
+
+/* record the swept pressure of the last interior plane before the reapply */
+static void save_p3(slab* S) {
+  long plane = (long)S->NX * S->NY;
+  memcpy(S->p3, S->p + (long)(S->NZ - 3) * plane, sizeof(double) * plane);
+}
+
+static void copy_state(slab* S) {
+  size_t n = sizeof(double) * S->NX * S->NY * S->NZ;
+  memcpy(S->u2, S->u, n); memcpy(S->v2, S->v, n);
+  memcpy(S->w2, S->w, n); memcpy(S->p2, S->p, n);
+}
+
+/* Ping-pong Jacobi ordering of the same update: every neighbour is read from
+ * the previous iterate; solvers 2/3 use the voxel's own new velocity in the
+ * divergence exactly as solver.cc:216-218 does. */
+static void sweep_jacobi(or_problem* pr, slab* S) {
+  copy_state(S);
+  for (int i = LIM; i < S->NZ - LIM; i++)
+    for (int j = LIM; j < S->NY - LIM; j++)
+      for (int k = LIM; k < S->NX - LIM; k++) {
+        long c = IDX(S, i, j, k);
+        if (S->g[c] == 0)
+          voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u2, S->v2, S->w2, S->p2,
+                i == S->NZ - 3 ? S->p3 : NULL);
+      }
+  swap_state(S);
+  save_p3(S);
+}
+
+/* Red-black ordering: colour = parity of the global interior coordinates.
+ * Red voxels update from the previous iterate; black voxels then update from
+ * the state holding the new red values and the old black values (so the
+ * same-colour +-2 reads of the wall stencils see old values and the result
+ * does not depend on the order inside a colour). */
+static void sweep_redblack(or_problem* pr, slab* S) {
+  copy_state(S); /* state2 := state */
+  for (int colour = 0; colour < 2; ++colour)
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++) {
+          if ((((k - LIM) + (j - LIM) + (S->z0 + i - LIM)) & 1) != colour) continue;
+          long c = IDX(S, i, j, k);
+          if (S->g[c] != 0) continue;
+          if (colour == 0) /* red: old state -> state2; black neighbours' swept p */
+            voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u2, S->v2, S->w2, S->p2,
+                  i == S->NZ - 3 ? S->p3 : NULL);
+          else /* black: state2 (new red, old black) -> state */
+            voxel(S, c, pr->solver, S->u2, S->v2, S->w2, S->p2, S->u, S->v, S->w, S->p, NULL);
+        }
+  /* merge the new red values into state */
+  for (int i = LIM; i < S->NZ - LIM; i++)
+    for (int j = LIM; j < S->NY - LIM; j++)
+      for (int k = LIM; k < S->NX - LIM; k++) {
+        if (((k - LIM) + (j - LIM) + (S->z0 + i - LIM)) & 1) continue;
+        long c = IDX(S, i, j, k);
+        if (S->g[c] != 0) continue;
+        S->u[c] = S->u2[c]; S->v[c] = S->v2[c]; S->w[c] = S->w2[c]; S->p[c] = S->p2[c];
+      }
+  save_p3(S);
+}
+
+typedef struct { or_problem* pr; int order; int first, step; } sweep_job;
+
+static void* sweep_worker(void* arg) {
+  sweep_job* jb = (sweep_job*)arg;
+  for (int c = jb->first; c < jb->pr->ns; c += jb->step) {
+    slab* S = &jb->pr->s[c];
+    if (jb->order == OR_ORDER_REFERENCE) sweep_reference(jb->pr, S);
+    else if (jb->order == OR_ORDER_JACOBI) sweep_jacobi(jb->pr, S);
+    else sweep_redblack(jb->pr, S);
+  }
+  return NULL;
+}
+
+static void sweep_all(or_problem* pr, int order) {
+  int nt = pr->nthreads < pr->ns ? pr->nthreads : pr->ns;
+  if (nt <= 1) {
+    sweep_job jb = {pr, order, 0, 1};
+    sweep_worker(&jb);
+    return;
+  }
+  pthread_t th[256];
+  sweep_job jobs[256];
+  if (nt > 256) nt = 256;
+  for (int t = 0; t < nt; ++t) {
+    jobs[t] = (sweep_job){pr, order, t, nt};
+    pthread_create(&th[t], NULL, sweep_worker, &jobs[t]);
+  }
+  for (int t = 0; t < nt; ++t) pthread_join(th[t], NULL);
+}
+
+/* ---------------------------------------------------------------------- */
+/* set-up: get_dom_limits (geometry.cc:129-171), read_geometry (:58-126),
+ * eval_geometry, allocate_initial_field (initialize.cc:69-121) and the
+ * periods of main_stokes_solver.cc:163-165. */
+or_problem* or_create(const int size[3], int bc_method, unsigned solver, int nslabs,
+                      const unsigned char* geom_raw, double voxel_size, double porosity,
+                      const int dom_interest[6]) {
+  if (nslabs < 1 || nslabs > size[2]) return NULL;
+  or_problem* pr = (or_problem*)calloc(1, sizeof(or_problem));
+  pr->nx = size[0]; pr->ny = size[1]; pr->nz = size[2];
+  pr->bc = bc_method; pr->solver = solver; pr->ns = nslabs;
+  pr->periods[0] = pr->periods[1] = (bc_method == 0);
+  pr->periods[2] = (bc_method <= 2);
+  pr->dx = voxel_size; pr->porosity_in = porosity;
+  for (int i = 0; i < 6; ++i) pr->di[i] = dom_interest ? dom_interest[i] : 0;
+  pr->nthreads = 1;
+  pr->s = (slab*)calloc(nslabs, sizeof(slab));
+  int base = size[2] / nslabs, add = size[2] - nslabs * base;
+  for (int c = 0; c < nslabs; ++c) {
+    slab* S = &pr->s[c];
+    int cum = c == 0 ? 0 : (c <= add ? c : add);
+    S->z0 = c * base + cum;
+    S->lnz = base + (c < add ? 1 : 0);
+    S->NX = size[0] + 4; S->NY = size[1] + 4; S->NZ = S->lnz + 4;
+    long n = (long)S->NX * S->NY * S->NZ;
+    S->g = (unsigned char*)calloc(n, 1);
+    S->nh = (int*)calloc(n, sizeof(int));
+    S->u = (double*)calloc(n, 8); S->v = (double*)calloc(n, 8);
+    S->w = (double*)calloc(n, 8); S->p = (double*)calloc(n, 8);
+    S->u2 = (double*)calloc(n, 8); S->v2 = (double*)calloc(n, 8);
+    S->w2 = (double*)calloc(n, 8); S->p2 = (double*)calloc(n, 8);
+    S->p3 = (double*)calloc((long)S->NX * S->NY, 8);
+    for (int i = 0; i < S->lnz; ++i)
+      for (int j = 0; j < size[1]; ++j)
+        for (int k = 0; k < size[0]; ++k)
+          S->g[IDX(S, i + 2, j + 2, k + 2)] =
+              geom_raw[((long)(S->z0 + i) * size[1] + j) * size[0] + k] != 0;
+  }
+  unsigned char** ga = (unsigned char**)malloc(sizeof(void*) * nslabs);
+  for (int c = 0; c < nslabs; ++c) ga[c] = pr->s[c].g;
+  exchange_u8(pr, ga);
+  free(ga);
+  for (int c = 0; c < nslabs; ++c) {
+    slab* S = &pr->s[c];
+    eval_geometry(S);
+    long n = (long)S->NX * S->NY * S->NZ;
+    for (long q = 0; q < n; ++q) S->p[q] = -1.0;
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++) {
+          long q = IDX(S, i, j, k);
+          S->p[q] = S->g[q] == 0 ? (double)((size[2] - S->z0 - i) + LIM + 2) : 0.0;
+        }
+  }
+  exchange_field(pr, 0);
+  for (int c = 0; c < nslabs; ++c) save_p3(&pr->s[c]);
+  /* set_halos_initial (initialize.cc:240-289) zeroes velocity halos that
+   * are already zero. */
+  pr->phi = porosity == -1.0 ? or_porosity(pr) : porosity;
+  pr->iteration = 0;
+  return pr;
+}
+
+void or_destroy(or_problem* pr) {
+  if (!pr) return;
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    free(S->g); free(S->nh);
+    free(S->u); free(S->v); free(S->w); free(S->p);
+    free(S->u2); free(S->v2); free(S->w2); free(S->p2);
+    free(S->p3);
+  }
+  free(pr->s);
+  free(pr);
+}
+
+int or_threads(or_problem* pr, int nthreads) {
+  pr->nthreads = nthreads < 1 ? 1 : nthreads;
+  return pr->nthreads;
+}
+
+/* get_porosity: geometry.cc:335-364 */
+double or_porosity(or_problem* pr) {
+  double fl = 0.0, vc = 0.0;
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    double f = 0.0;
+    double v = (S->NX - 2 * LIM) * (S->NY - 2 * LIM) * (S->NZ - 2 * LIM);
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++)
+          if (S->g[IDX(S, i, j, k)] == 0) f += 1.0;
+    fl = c == 0 ? f : fl + f;
+    vc = c == 0 ? v : vc + v;
+  }
+  return fl / vc;
+}
+
+/* compute_convergence: evaluation.cc:216-262 */
+double or_convergence(or_problem* pr, double* permeability) {
+  double sum = 0.0, cnt = 0.0;
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    double vs = 0.0;
+    int fl = 0;
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++) {
+          long q = IDX(S, i, j, k);
+          if (S->g[q] == 0) { fl += 1; vs += S->w[q]; }
+        }
+    if (fl == 0) vs = 0.0;
+    if (c == 0) { sum = vs; cnt = (double)fl; }
+    else { sum = sum + vs; cnt = cnt + (double)fl; }
+  }
+  int flcount = (int)cnt;
+  double mean = sum / flcount;
+  double cur = mean / RE;
+  double conv = fabs(cur - *permeability) / cur;
+  *permeability = cur;
+  return conv;
+}
+
+/* compute_permeability: evaluation.cc:54-211 */
+void or_permeability(or_problem* pr, or_result* res) {
+  double W[3] = {0, 0, 0}, wmax = 0.0;
+  int wfl = 0;
+  double D[5] = {0, 0, 0, 0, 0};
+  int I[3] = {0, 0, 0};
+  const int* di = pr->di;
+  int dofi = !(di[0] == 0 && di[1] == 0 && di[2] == 0 && di[3] == 0 && di[4] == 0 && di[5] == 0);
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    double wx = 0, wy = 0, wz = 0, wm = 0.0, vx = 0, vy = 0, vz = 0, p0 = 0, pe = 0;
+    int wf = 0, fl = 0, p0f = 0, pef = 0;
+    for (int i = LIM; i < S->NZ - LIM; i++)
+      for (int j = LIM; j < S->NY - LIM; j++)
+        for (int k = LIM; k < S->NX - LIM; k++) {
+          long q = IDX(S, i, j, k);
+          if (S->g[q] == 0) {
+            wf += 1; wx += S->u[q]; wy += S->v[q]; wz += S->w[q];
+            if (S->w[q] > wm) wm = S->w[q];
+          }
+        }
+    if (dofi)
+      for (int i = LIM; i < S->NZ - LIM; i++)
+        for (int j = LIM; j < S->NY - LIM; j++)
+          for (int k = LIM; k < S->NX - LIM; k++) {
+            int gi = S->z0 + i - LIM, gj = j - LIM, gk = k - LIM;
+            if (gk < di[0] || gk > di[1] || gj < di[2] || gj > di[3] || gi < di[4] || gi > di[5])
+              continue;
+            long q = IDX(S, i, j, k);
+            if (S->g[q] == 0) { fl += 1; vx += S->u[q]; vy += S->v[q]; vz += S->w[q]; }
+            if (gi == di[4] && S->g[q] == 0) { p0f += 1; p0 += S->p[q]; }
+            if (gi == di[5] && S->g[q] == 0) { pef += 1; pe += S->p[q]; }
+          }
+    if (wf == 0) { wx = wy = wz = 0.0; wm = 0.0; }
+    if (fl == 0) { vx = vy = vz = 0.0; }
+    if (p0f == 0) p0 = 0.0;
+    if (pef == 0) pe = 0.0;
+    double d5[5] = {vx, vy, vz, p0, pe};
+    int i3[3] = {fl, p0f, pef};
+    for (int t = 0; t < 5; ++t) D[t] = c == 0 ? d5[t] : D[t] + d5[t];
+    for (int t = 0; t < 3; ++t) I[t] = c == 0 ? i3[t] : I[t] + i3[t];
+    double w3[3] = {wx, wy, wz};
+    for (int t = 0; t < 3; ++t) W[t] = c == 0 ? w3[t] : W[t] + w3[t];
+    wfl = c == 0 ? wf : wfl + wf;
+    wmax = c == 0 ? wm : (wm > wmax ? wm : wmax);
+  }
+  double phi = pr->phi, dx = pr->dx;
+  if (dofi) {
+    double pgrad = ((D[4] / I[2]) - (D[3] / I[1])) / (di[5] - di[4]);
+    res->k13 = (D[0] / I[0]) * (1.0 / RE) * phi * (1.0 / pgrad) * (dx * dx);
+    res->k23 = (D[1] / I[0]) * (1.0 / RE) * phi * (1.0 / pgrad) * (dx * dx);
+    res->k33 = (D[2] / I[0]) * (1.0 / RE) * phi * (1.0 / pgrad) * (dx * dx);
+  } else {
+    res->k13 = res->k23 = res->k33 = 0.0;
+  }
+  res->wk13 = (W[0] / wfl) * (1.0 / RE) * phi * (dx * dx);
+  res->wk23 = (W[1] / wfl) * (1.0 / RE) * phi * (dx * dx);
+  res->wk33 = (W[2] / wfl) * (1.0 / RE) * phi * (dx * dx);
+  res->wmean_velz = W[2] / wfl * dx;
+  res->wmax_velz = wmax * dx;
+  res->porosity = phi;
+}
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void one_iteration(or_problem* pr, int order) {
+  if (pr->iteration == 0) reapply(pr);
+  sweep_all(pr, order);
+  for (int f = 0; f < 4; ++f) exchange_field(pr, f);
+  reapply(pr);
+}
+
+void or_iterate(or_problem* pr, int order, int n) {
+  for (int t = 0; t < n; ++t) {
+    one_iteration(pr, order);
+    pr->iteration++;
+  }
+}
+
+/* calc_flow: calc_flow.cc:53-169, including the log rows of output.cc:193-230 */
+void or_calc_flow(or_problem* pr, int order, int max_iter, int it_eval, int it_write, double eps,
+                  const char* log_path, or_result* res) {
+  double conv = 1.0 + eps, perm = 0.0;
+  int first = 1;
+  memset(res, 0, sizeof(*res));
+  while (pr->iteration < max_iter && conv >= eps) {
+    int it = pr->iteration;
+    double t0 = now_s();
+    one_iteration(pr, order);
+    if (it % it_eval == 0 && it > 1000) {
+      conv = or_convergence(pr, &perm);
+      if (it % it_write == 0) {
+        or_permeability(pr, res);
+        if (log_path) {
+          double tps = 1.0 / (now_s() - t0);
+          FILE* f = fopen(log_path, "a");
+          if (f) {
+            if (first)
+              fprintf(f, "# iteration, conv, TPS [1/s], wmax_velz [m/s], wmean_velz [m/s], k13 "
+                         "[m^2], k23 [m^2], k33 [m^2], wk13 [m^2], wk23 [m^2], wk33 [m^2]\n");
+            fprintf(f, "%i, %e, %e, %e, %e, %e, %e, %e, %e, %e, %e\n", it, conv, tps,
+                    res->wmax_velz, res->wmean_velz, res->k13, res->k23, res->k33, res->wk13,
+                    res->wk23, res->wk33);
+            fclose(f);
+          }
+        }
+        first = 0;
+      }
+      res->iterations = it;
+    }
+    pr->iteration++;
+  }
+  /* the result reports the permeability of the final state (the log rows keep
+   * the values of their own iterations) */
+  int last = res->iterations;
+  or_permeability(pr, res);
+  res->iterations = last;
+  res->sweeps = pr->iteration;
+  res->conv = conv;
+  res->permeability = perm;
+  res->porosity = pr->phi;
+}
+
+void or_get_fields(const or_problem* pr, double* u, double* v, double* w, double* p) {
+  for (int c = 0; c < pr->ns; ++c) {
+    const slab* S = &pr->s[c];
+    for (int i = 0; i < S->lnz; ++i)
+      for (int j = 0; j < pr->ny; ++j)
+        for (int k = 0; k < pr->nx; ++k) {
+          long o = ((long)(S->z0 + i) * pr->ny + j) * pr->nx + k;
+          long q = IDX(S, i + 2, j + 2, k + 2);
+          if (u) u[o] = S->u[q];
+          if (v) v[o] = S->v[q];
+          if (w) w[o] = S->w[q];
+          if (p) p[o] = S->p[q];
+        }
+  }
+}
+
+void or_get_nhood(const or_problem* pr, int* out) {
+  for (int c = 0; c < pr->ns; ++c) {
+    const slab* S = &pr->s[c];
+    for (int i = 0; i < S->lnz; ++i)
+      for (int j = 0; j < pr->ny; ++j)
+        for (int k = 0; k < pr->nx; ++k)
+          out[((long)(S->z0 + i) * pr->ny + j) * pr->nx + k] = S->nh[IDX(S, i + 2, j + 2, k + 2)];
+  }
+}
+
+void or_get_padded(const or_problem* pr, int s, int dims_out[3], double* u, double* v, double* w,
+                   double* p) {
+  const slab* S = &pr->s[s];
+  dims_out[0] = S->NX; dims_out[1] = S->NY; dims_out[2] = S->NZ;
+  size_t n = sizeof(double) * S->NX * S->NY * S->NZ;
+  if (u) memcpy(u, S->u, n);
+  if (v) memcpy(v, S->v, n);
+  if (w) memcpy(w, S->w, n);
+  if (p) memcpy(p, S->p, n);
+}

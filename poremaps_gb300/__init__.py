@@ -1,0 +1,315 @@
+"""poremaps_gb300 -- GB300 (sm_103a) POREMAPS pseudo-time Stokes permeability solver.
+
+Python front-end over the C ABI of ``include/poremaps.h`` (ctypes).  All
+compute runs in the native library ``_build/libporemaps_gb300.so``; there is
+no CPU fallback: importing this package without the built library raises.
+
+Mirror of the reference program's interface (krachdd/poremaps):
+  read_params      <- read_problem_params (src/read_problem_params.cc:50-156)
+  Problem          <- the state set up in src/main_stokes_solver.cc:195-276
+  Problem.solve    <- calc_flow (src/calc_flow.cc:53-169)
+  Problem.iterate  <- one calc_flow iteration (central_diff5 + halo exchange + reapply)
+  Problem.convergence / permeability <- src/evaluation.cc:54-262
+  run_inp          <- the POREMAPS program (src/main_stokes_solver.cc:57-416)
+  solve_tensor     <- the three axis-rotated runs of README.md:215-227
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libporemaps_gb300.so")
+CLI_PATH = os.path.join(HERE, "_build", "poremaps_gpu")
+
+ORDER_DEFAULT, ORDER_REFERENCE, ORDER_JACOBI, ORDER_REDBLACK = -1, 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+ARITH_EXACT, ARITH_FAST = 0, 1
+ORDERS = {"default": -1, "reference": 0, "jacobi": 1, "redblack": 2}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+ARITHS = {"exact": 0, "fast": 1}
+
+STATUS = {0: "PM_OK", 1: "PM_ERR_INVALID", 2: "PM_ERR_IO", 3: "PM_ERR_CUDA", 4: "PM_ERR_NOMEM",
+          5: "PM_ERR_NONFINITE", 6: "PM_ERR_BUSY", 7: "PM_ERR_NOT_FOUND"}
+
+
+class PMError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("dom_decomposition", C.c_int * 3), ("boundary_method", C.c_int),
+                ("geometry_file_name", C.c_char * 400), ("size", C.c_int * 3),
+                ("voxel_size", C.c_double), ("max_iter", C.c_int), ("it_eval", C.c_int),
+                ("it_write", C.c_int), ("log_file_name", C.c_char * 400),
+                ("solving_algorithm", C.c_uint), ("eps", C.c_double), ("porosity", C.c_double),
+                ("dom_interest", C.c_int * 6), ("write_output", C.c_int * 4),
+                ("order", C.c_int), ("precision", C.c_int), ("arith", C.c_int),
+                ("write_log", C.c_int), ("mixed_inner", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("sweeps", C.c_int), ("converged", C.c_int),
+                ("conv", C.c_double), ("permeability", C.c_double), ("k13", C.c_double),
+                ("k23", C.c_double), ("k33", C.c_double), ("wk13", C.c_double),
+                ("wk23", C.c_double), ("wk33", C.c_double), ("wmax_velz", C.c_double),
+                ("wmean_velz", C.c_double), ("porosity", C.c_double), ("device_ms", C.c_double),
+                ("wall_ms", C.c_double), ("glups", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int),
+                ("precision", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("result", Result),
+                ("submit_ms", C.c_double), ("admit_ms", C.c_double), ("finish_ms", C.c_double)]
+
+
+# Every symbol declared in include/poremaps.h (checked by the CPU tests).
+EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
+           "pm_read_geometry", "pm_problem_create", "pm_problem_destroy", "pm_solve",
+           "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
+           "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
+           "pm_run_inp", "pm_solve_tensor", "pm_server_create", "pm_server_destroy",
+           "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
+           "pm_server_clock_ms"]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"poremaps_gb300 native library missing: {path} "
+                          "(run __graft_entry__.build() or python poremaps_gb300/build.py)")
+    L = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    sig = {
+        "pm_last_error": (C.c_char_p, []),
+        "pm_version": (C.c_char_p, []),
+        "pm_params_default": (C.c_int, [P(Params)]),
+        "pm_read_params": (C.c_int, [C.c_char_p, P(Params)]),
+        "pm_read_geometry": (C.c_int, [C.c_char_p, P(C.c_int), vp]),
+        "pm_problem_create": (C.c_int, [P(Params), vp, P(vp)]),
+        "pm_problem_destroy": (C.c_int, [vp]),
+        "pm_solve": (C.c_int, [vp, P(Result)]),
+        "pm_iterate": (C.c_int, [vp, C.c_int]),
+        "pm_compute_convergence": (C.c_int, [vp, P(C.c_double), P(C.c_double)]),
+        "pm_compute_permeability": (C.c_int, [vp, P(Result)]),
+        "pm_get_porosity": (C.c_int, [vp, P(C.c_double)]),
+        "pm_get_iteration": (C.c_int, [vp, P(C.c_int)]),
+        "pm_get_fields": (C.c_int, [vp, vp, vp, vp, vp]),
+        "pm_get_neighborhood": (C.c_int, [vp, vp]),
+        "pm_write_outputs": (C.c_int, [vp]),
+        "pm_run_inp": (C.c_int, [C.c_char_p, P(Params), P(Result)]),
+        "pm_solve_tensor": (C.c_int, [P(Params), vp, P(C.c_double), P(Result)]),
+        "pm_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
+        "pm_server_destroy": (C.c_int, [vp]),
+        "pm_server_submit": (C.c_int, [vp, P(Params), vp, P(C.c_uint64)]),
+        "pm_server_step": (C.c_int, [vp, P(C.c_int)]),
+        "pm_server_poll": (C.c_int, [vp, P(Completion), C.c_int, P(C.c_int)]),
+        "pm_server_stats": (C.c_int, [vp, P(C.c_double), P(C.c_double), P(C.c_uint64)]),
+        "pm_server_clock_ms": (C.c_double, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(L, name):
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(st: int):
+    if st != 0:
+        raise PMError(st, load_library().pm_last_error().decode(errors="replace"))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    _check(load_library().pm_params_default(C.byref(p)))
+    for k, v in kw.items():
+        if k == "order" and isinstance(v, str):
+            v = ORDERS[v]
+        if k == "precision" and isinstance(v, str):
+            v = PRECISIONS[v]
+        if k == "arith" and isinstance(v, str):
+            v = ARITHS[v]
+        if k in ("geometry_file_name", "log_file_name"):
+            v = v.encode() if isinstance(v, str) else v
+        if k in ("size", "dom_interest", "write_output", "dom_decomposition"):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+            continue
+        setattr(p, k, v)
+    return p
+
+
+def read_params(path: str) -> Params:
+    p = Params()
+    _check(load_library().pm_read_params(path.encode(), C.byref(p)))
+    return p
+
+
+class Problem:
+    """One device-resident domain.  ``geom``: (nz, ny, nx) uint8 (x fastest,
+    0 fluid, nonzero solid)."""
+
+    def __init__(self, geom: np.ndarray, params: Params | None = None, **kw):
+        g = np.ascontiguousarray(geom, dtype=np.uint8)
+        nz, ny, nx = g.shape
+        if params is None:
+            params = default_params(**kw)
+        else:
+            params = Params.from_buffer_copy(params)
+            for k, v in kw.items():
+                setattr(params, k, ORDERS.get(v, v) if k == "order" and isinstance(v, str) else v)
+        params.size[0], params.size[1], params.size[2] = nx, ny, nz
+        self.params = params
+        self.shape = g.shape
+        self.h = C.c_void_p()
+        _check(load_library().pm_problem_create(C.byref(params), g.ctypes.data, C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            load_library().pm_problem_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, n: int) -> None:
+        _check(load_library().pm_iterate(self.h, n))
+
+    def solve(self) -> Result:
+        r = Result()
+        st = load_library().pm_solve(self.h, C.byref(r))
+        if st not in (0, 5):
+            _check(st)
+        return r
+
+    def convergence(self, permeability: float = 0.0):
+        p = C.c_double(permeability)
+        c = C.c_double()
+        _check(load_library().pm_compute_convergence(self.h, C.byref(p), C.byref(c)))
+        return c.value, p.value
+
+    def permeability(self) -> Result:
+        r = Result()
+        _check(load_library().pm_compute_permeability(self.h, C.byref(r)))
+        return r
+
+    def porosity(self) -> float:
+        v = C.c_double()
+        _check(load_library().pm_get_porosity(self.h, C.byref(v)))
+        return v.value
+
+    def fields(self):
+        arr = [np.empty(self.shape, np.float64) for _ in range(4)]
+        _check(load_library().pm_get_fields(self.h, *[a.ctypes.data for a in arr]))
+        return arr  # u, v, w, p
+
+    def nhood(self) -> np.ndarray:
+        out = np.empty(self.shape, np.int32)
+        _check(load_library().pm_get_neighborhood(self.h, out.ctypes.data))
+        return out
+
+    def write_outputs(self) -> None:
+        _check(load_library().pm_write_outputs(self.h))
+
+
+def run_inp(path: str, **overrides) -> Result:
+    ov = default_params(**overrides)
+    r = Result()
+    st = load_library().pm_run_inp(path.encode(), C.byref(ov), C.byref(r))
+    if st not in (0, 5):
+        _check(st)
+    return r
+
+
+def solve_tensor(geom: np.ndarray, params: Params | None = None, **kw):
+    """Full permeability tensor K (3x3, m^2; K[i, j] = response along axis i to
+    the pressure drop along axis j) from three axis-rotated solves."""
+    g = np.ascontiguousarray(geom, dtype=np.uint8)
+    nz, ny, nx = g.shape
+    p = default_params(**kw) if params is None else Params.from_buffer_copy(params)
+    p.size[0], p.size[1], p.size[2] = nx, ny, nz
+    K = (C.c_double * 9)()
+    res = (Result * 3)()
+    st = load_library().pm_solve_tensor(C.byref(p), g.ctypes.data, K, res)
+    if st not in (0, 5):
+        _check(st)
+    return np.array(list(K)).reshape(3, 3), list(res)
+
+
+class Server:
+    """Batched / continuously batching solver (pm_server_* of the C ABI)."""
+
+    def __init__(self, precision: str | int = "mixed", hbm_budget_bytes: int = 0,
+                 max_resident: int = 0, use_graphs: int = 1, autotune: int = 0):
+        cfg = ServerConfig(hbm_budget_bytes, max_resident,
+                           PRECISIONS.get(precision, precision), use_graphs, autotune)
+        self.h = C.c_void_p()
+        _check(load_library().pm_server_create(C.byref(cfg), C.byref(self.h)))
+
+    def submit(self, geom: np.ndarray, params: Params | None = None, **kw) -> int:
+        g = np.ascontiguousarray(geom, dtype=np.uint8)
+        nz, ny, nx = g.shape
+        p = default_params(**kw) if params is None else Params.from_buffer_copy(params)
+        p.size[0], p.size[1], p.size[2] = nx, ny, nz
+        t = C.c_uint64()
+        _check(load_library().pm_server_submit(self.h, C.byref(p), g.ctypes.data, C.byref(t)))
+        return t.value
+
+    def step(self) -> int:
+        a = C.c_int()
+        _check(load_library().pm_server_step(self.h, C.byref(a)))
+        return a.value
+
+    def poll(self, max_n: int = 256):
+        buf = (Completion * max_n)()
+        n = C.c_int()
+        _check(load_library().pm_server_poll(self.h, buf, max_n, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def stats(self):
+        b, w, l = C.c_double(), C.c_double(), C.c_uint64()
+        _check(load_library().pm_server_stats(self.h, C.byref(b), C.byref(w), C.byref(l)))
+        return b.value, w.value, l.value
+
+    def clock_ms(self) -> float:
+        return load_library().pm_server_clock_ms(self.h)
+
+    def close(self):
+        if self.h:
+            load_library().pm_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,524 @@
+// Host runtime and C ABI of poremaps_gb300 (see include/poremaps.h).
+//
+// The calc_flow loop (reference src/calc_flow.cc:53-169) runs on the host and
+// drives device sweeps in blocks that end exactly at the iterations where the
+// reference evaluates convergence (it % it_eval == 0 && it > 1000), so the
+// stopping iteration, the log rows and the final fields follow the reference's
+// control flow.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <chrono>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/poremaps.h"
+#include "pm_api_internal.h"
+#include "pm_internal.h"
+
+using namespace pm;
+
+namespace {
+
+thread_local std::string g_err;
+
+}  // namespace
+
+namespace pm {
+
+pm_status set_error(pm_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return st;
+}
+
+pm_status cuda_error(cudaError_t e, const char* where) {
+  if (e == cudaErrorMemoryAllocation)
+    return set_error(PM_ERR_NOMEM, "%s: %s", where, cudaGetErrorString(e));
+  return set_error(PM_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+}  // namespace pm
+
+#define CK(expr)                                        \
+  do {                                                  \
+    cudaError_t _e = (expr);                            \
+    if (_e != cudaSuccess) return cuda_error(_e, #expr); \
+  } while (0)
+
+// ------------------------------------------------------------------ problem
+struct pm_problem {
+  pm_params prm;
+  Grid g;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int order = PM_ORDER_JACOBI;
+  int precision = PM_PREC_FP64;
+  int solver = 2;
+  int exact = 1;
+  // device memory
+  uint8_t* codes_base = nullptr;
+  uint8_t* codes = nullptr;
+  int* list = nullptr;
+  int nlist = 0;
+  double* f64_base[2] = {nullptr, nullptr};
+  Fields<double> F[2];
+  float* f32_base = nullptr;  // e0, e1, r
+  Fields<float> E[2], R;
+  double* partials = nullptr;
+  double* dout = nullptr;
+  double* hout = nullptr;  // pinned
+  void* scratch = nullptr;  // export buffer
+  size_t scratch_bytes = 0;
+  int coop_blocks = 0;
+  // state
+  int cur = 0;        // FP64 state buffer holding the current iterate
+  int ecur = 0;       // FP32 correction buffer holding e
+  int dc_pos = 0;     // sweeps since the last FP64 correction (mixed form)
+  int mixed_inner = 100;
+  int iteration = 0;  // next iteration index of calc_flow
+  double perm_prev = 0.0;
+  double conv = 0.0;
+  bool conv_valid = false;
+  bool first_log = true;
+  Counts counts{};
+  double phi = 0.0;
+  double device_ms = 0.0;
+  long long sweeps_done = 0;
+};
+
+namespace {
+
+long long align_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+pm_status validate(const pm_params* p) {
+  if (!p) return set_error(PM_ERR_INVALID, "params is NULL");
+  if (p->size[0] < 1 || p->size[1] < 1 || p->size[2] < 1)
+    return set_error(PM_ERR_INVALID, "size_x_y_z must be positive (got %d %d %d)", p->size[0],
+                     p->size[1], p->size[2]);
+  if ((long long)p->size[0] * p->size[1] * p->size[2] > (1LL << 31) - 1)
+    return set_error(PM_ERR_INVALID, "domain larger than 2^31 voxels");
+  if (p->boundary_method < 0 || p->boundary_method > 4)
+    return set_error(PM_ERR_INVALID, "boundary_method must be 0..4 (got %d)", p->boundary_method);
+  if (p->solving_algorithm < 1 || p->solving_algorithm > 3)
+    return set_error(PM_ERR_INVALID, "solving_algorithm must be 1, 2 or 3 (got %u)",
+                     p->solving_algorithm);
+  if (p->it_eval <= 0 || p->it_write <= 0)
+    return set_error(PM_ERR_INVALID, "it_eval and it_write must be positive");
+  if (p->order < -1 || p->order > 2) return set_error(PM_ERR_INVALID, "bad order %d", p->order);
+  if (p->precision < 0 || p->precision > 1)
+    return set_error(PM_ERR_INVALID, "bad precision %d", p->precision);
+  if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
+    return set_error(PM_ERR_INVALID,
+                     "mixed precision sweeps in Jacobi order, which diverges for solver 1 "
+                     "(explicit pressure update); use solver 2/3 or precision fp64");
+  return PM_OK;
+}
+
+pm_status device_sync(pm_problem* pr, const char* where) {
+  cudaError_t e = cudaStreamSynchronize(pr->st);
+  if (e != cudaSuccess) return cuda_error(e, where);
+  return PM_OK;
+}
+
+// One iteration of the FP64 forms: sweep A -> B (fused exchange + reapply), swap.
+pm_status iterate64(pm_problem* pr) {
+  Fields<double> A = pr->F[pr->cur], B = pr->F[1 - pr->cur];
+  if (pr->order == PM_ORDER_JACOBI) {
+    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
+                      pr->st));
+  } else {
+    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 1,
+                      pr->st));
+    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 2,
+                      pr->st));
+  }
+  pr->cur = 1 - pr->cur;
+  return PM_OK;
+}
+
+pm_status dc_flush(pm_problem* pr) {
+  if (pr->dc_pos > 0) {
+    CK(launch_dc_correct(pr->F[pr->cur], pr->E[pr->ecur], pr->g, pr->st));
+    pr->dc_pos = 0;
+  }
+  return PM_OK;
+}
+
+pm_status iterate_mixed(pm_problem* pr) {
+  if (pr->dc_pos == 0) {
+    CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list, pr->nlist,
+                          pr->g, pr->solver, pr->st));
+  } else {
+    CK(launch_dc_inner(pr->E[pr->ecur], pr->E[1 - pr->ecur], pr->R, pr->codes, pr->list,
+                       pr->nlist, pr->g, pr->solver, pr->st));
+    pr->ecur = 1 - pr->ecur;
+  }
+  pr->dc_pos++;
+  if (pr->dc_pos >= pr->mixed_inner) return dc_flush(pr);
+  return PM_OK;
+}
+
+pm_status iterate_n(pm_problem* pr, int n) {
+  if (n <= 0) return PM_OK;
+  if (pr->order == PM_ORDER_REFERENCE) {
+    CK(launch_wavefront(pr->F[pr->cur], pr->codes, pr->g, pr->solver, n, &pr->coop_blocks,
+                        pr->st));
+  } else {
+    for (int i = 0; i < n; ++i) {
+      pm_status s = pr->precision == PM_PREC_MIXED ? iterate_mixed(pr) : iterate64(pr);
+      if (s != PM_OK) return s;
+    }
+  }
+  pr->iteration += n;
+  pr->sweeps_done += n;
+  return PM_OK;
+}
+
+pm_status reduce(pm_problem* pr, int full) {
+  int mode = (pr->precision == PM_PREC_MIXED && pr->dc_pos > 0) ? 1 : 0;
+  CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
+                   pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
+                   pr->prm.dom_interest, pr->partials, pr->dout, pr->st));
+  CK(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(double) * kRedVals, cudaMemcpyDeviceToHost,
+                     pr->st));
+  return device_sync(pr, "reduce");
+}
+
+// compute_convergence (evaluation.cc:216-262)
+void convergence_from(pm_problem* pr, double velz_sum, double* perm, double* conv) {
+  int flcount = (int)(double)pr->counts.fluid;
+  double sum = flcount == 0 ? 0.0 : velz_sum;
+  double mean = sum / flcount;
+  double cur = mean / kRe;
+  *conv = fabs(cur - *perm) / cur;
+  *perm = cur;
+}
+
+// compute_permeability (evaluation.cc:54-211) from the device sums
+void permeability_from(pm_problem* pr, const double* s, pm_result* r) {
+  const int* di = pr->prm.dom_interest;
+  bool dofi = di[0] | di[1] | di[2] | di[3] | di[4] | di[5];
+  int wfl = (int)pr->counts.fluid;
+  double wx = s[0], wy = s[1], wz = s[2], wmax = s[3];
+  if (wfl == 0) { wx = wy = wz = 0.0; wmax = 0.0; }
+  double phi = pr->phi, dx = pr->prm.voxel_size;
+  if (dofi) {
+    int fl = (int)pr->counts.box_fluid, p0f = (int)pr->counts.p0_fluid,
+        pef = (int)pr->counts.pend_fluid;
+    double vx = fl ? s[4] : 0.0, vy = fl ? s[5] : 0.0, vz = fl ? s[6] : 0.0;
+    double p0 = p0f ? s[7] : 0.0, pe = pef ? s[8] : 0.0;
+    double pgrad = ((pe / pef) - (p0 / p0f)) / (di[5] - di[4]);
+    r->k13 = (vx / fl) * (1.0 / kRe) * phi * (1.0 / pgrad) * (dx * dx);
+    r->k23 = (vy / fl) * (1.0 / kRe) * phi * (1.0 / pgrad) * (dx * dx);
+    r->k33 = (vz / fl) * (1.0 / kRe) * phi * (1.0 / pgrad) * (dx * dx);
+  } else {
+    r->k13 = r->k23 = r->k33 = 0.0;
+  }
+  r->wk13 = (wx / wfl) * (1.0 / kRe) * phi * (dx * dx);
+  r->wk23 = (wy / wfl) * (1.0 / kRe) * phi * (dx * dx);
+  r->wk33 = (wz / wfl) * (1.0 / kRe) * phi * (dx * dx);
+  r->wmean_velz = wz / wfl * dx;
+  r->wmax_velz = wmax * dx;
+  r->porosity = phi;
+}
+
+}  // namespace
+
+namespace pm {
+
+// write_logfile (output.cc:193-230): same header and "%i, %e, ..." row format.
+pm_status write_log_row(const char* path, bool first, int iteration, double conv, double tps,
+                        const pm_result& r) {
+  FILE* f = fopen(path, "a");
+  if (!f) return set_error(PM_ERR_IO, "cannot open log file %s", path);
+  if (first)
+    fprintf(f,
+            "# iteration, conv, TPS [1/s], wmax_velz [m/s], wmean_velz [m/s], k13 [m^2], k23 "
+            "[m^2], k33 [m^2], wk13 [m^2], wk23 [m^2], wk33 [m^2]\n");
+  fprintf(f, "%i, %e, %e, %e, %e, %e, %e, %e, %e, %e, %e\n", iteration, conv, tps, r.wmax_velz,
+          r.wmean_velz, r.k13, r.k23, r.k33, r.wk13, r.wk23, r.wk33);
+  fclose(f);
+  return PM_OK;
+}
+
+size_t problem_device_bytes(const pm_params* p) {
+  Grid g = make_grid(p->size[0], p->size[1], p->size[2], p->boundary_method);
+  size_t b = (size_t)g.allocc + 4 * (size_t)g.nvox + 2 * 4 * 8 * (size_t)g.alloc64;
+  if (p->precision == PM_PREC_MIXED) b += 3 * 4 * 4 * (size_t)g.alloc32;
+  b += 8 * (size_t)g.nvox;  // export scratch
+  return b + (1 << 20);
+}
+
+}  // namespace pm
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+const char* pm_last_error(void) { return g_err.c_str(); }
+const char* pm_version(void) { return "poremaps_gb300 0.1 (sm_103a)"; }
+
+pm_status pm_params_default(pm_params* p) {
+  if (!p) return set_error(PM_ERR_INVALID, "params is NULL");
+  memset(p, 0, sizeof(*p));
+  p->boundary_method = 0;
+  p->voxel_size = 1e-5;
+  p->max_iter = 100000001;
+  p->it_eval = 100;
+  p->it_write = 100;
+  p->solving_algorithm = 2;
+  p->eps = 1e-6;
+  p->porosity = -1.0;
+  p->order = PM_ORDER_DEFAULT;
+  p->precision = PM_PREC_FP64;
+  p->arith = PM_ARITH_FAST;
+  p->write_log = 0;
+  p->mixed_inner = 0;
+  return PM_OK;
+}
+
+pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem** out) {
+  if (!out) return set_error(PM_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  pm_status s = validate(p);
+  if (s != PM_OK) return s;
+  if (!geom) return set_error(PM_ERR_INVALID, "geometry is NULL");
+  pm_problem* pr = new pm_problem();
+  pr->prm = *p;
+  pr->solver = (int)p->solving_algorithm;
+  pr->order = p->order == PM_ORDER_DEFAULT ? PM_ORDER_REDBLACK : p->order;
+  pr->precision = p->precision;
+  if (pr->precision == PM_PREC_MIXED) pr->order = PM_ORDER_JACOBI;
+  if (pr->order == PM_ORDER_REFERENCE) pr->precision = PM_PREC_FP64;
+  pr->exact = p->arith == PM_ARITH_EXACT;
+  pr->mixed_inner = p->mixed_inner > 0 ? p->mixed_inner : p->it_eval;
+  pr->g = make_grid(p->size[0], p->size[1], p->size[2], p->boundary_method);
+  const Grid& g = pr->g;
+  auto fail = [&](pm_status st) {
+    pm_problem_destroy(pr);
+    return st;
+  };
+  size_t need = problem_device_bytes(p);
+  size_t freeb = 0, totalb = 0;
+  if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess)
+    return fail(cuda_error(cudaGetLastError(), "cudaMemGetInfo"));
+  if (need > freeb)
+    return fail(set_error(PM_ERR_NOMEM, "problem needs %zu bytes, %zu free", need, freeb));
+  cudaError_t e;
+#define CKF(expr)                                              \
+  do {                                                         \
+    if ((e = (expr)) != cudaSuccess) return fail(cuda_error(e, #expr)); \
+  } while (0)
+  CKF(cudaStreamCreateWithFlags(&pr->st, cudaStreamNonBlocking));
+  CKF(cudaEventCreate(&pr->ev0));
+  CKF(cudaEventCreate(&pr->ev1));
+  CKF(cudaMalloc((void**)&pr->codes_base, g.allocc));
+  pr->codes = pr->codes_base + kXoffC;
+  CKF(cudaMemsetAsync(pr->codes_base, 0, g.allocc, pr->st));
+  CKF(cudaMalloc((void**)&pr->list, sizeof(int) * (size_t)(g.nvox > 0 ? g.nvox : 1)));
+  for (int b = 0; b < 2; ++b) {
+    CKF(cudaMalloc((void**)&pr->f64_base[b], 4 * sizeof(double) * (size_t)g.alloc64));
+    double* base = pr->f64_base[b];
+    pr->F[b] = {base + kXoff64, base + g.alloc64 + kXoff64, base + 2 * g.alloc64 + kXoff64,
+                base + 3 * g.alloc64 + kXoff64};
+  }
+  if (pr->precision == PM_PREC_MIXED) {
+    CKF(cudaMalloc((void**)&pr->f32_base, 12 * sizeof(float) * (size_t)g.alloc32));
+    CKF(cudaMemsetAsync(pr->f32_base, 0, 12 * sizeof(float) * (size_t)g.alloc32, pr->st));
+    float* b = pr->f32_base;
+    for (int k = 0; k < 3; ++k) {
+      Fields<float> f = {b + (4 * k) * g.alloc32 + kXoff32, b + (4 * k + 1) * g.alloc32 + kXoff32,
+                         b + (4 * k + 2) * g.alloc32 + kXoff32,
+                         b + (4 * k + 3) * g.alloc32 + kXoff32};
+      if (k < 2) pr->E[k] = f;
+      else pr->R = f;
+    }
+  } else {
+    pr->E[0] = pr->E[1] = pr->R = {nullptr, nullptr, nullptr, nullptr};
+  }
+  CKF(cudaMalloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
+  CKF(cudaMalloc((void**)&pr->dout, sizeof(double) * 16));
+  CKF(cudaMallocHost((void**)&pr->hout, sizeof(double) * 16));
+  pr->scratch_bytes = 8 * (size_t)g.nvox;
+  CKF(cudaMalloc(&pr->scratch, pr->scratch_bytes));
+  // geometry upload (through the export scratch) -> codes -> fluid list
+  CKF(cudaMemcpyAsync(pr->scratch, geom, (size_t)g.nvox, cudaMemcpyHostToDevice, pr->st));
+  CKF(launch_codes((const uint8_t*)pr->scratch, pr->codes, g, pr->st));
+  int* dcount = (int*)pr->dout;
+  CKF(launch_fluid_list(pr->codes, g, pr->list, dcount, pr->st));
+  unsigned long long* dcnt = (unsigned long long*)((char*)pr->dout + 64);
+  CKF(launch_counts(pr->codes, g, p->dom_interest, dcnt, pr->st));
+  CKF(cudaMemcpyAsync(pr->hout, pr->dout, 96, cudaMemcpyDeviceToHost, pr->st));
+  CKF(launch_init64(pr->F[0], pr->codes, g, pr->st));
+  CKF(launch_copy_fields64(pr->F[1], pr->F[0], g, pr->st));
+  CKF(cudaStreamSynchronize(pr->st));
+  pr->nlist = *(int*)pr->hout;
+  unsigned long long* hc = (unsigned long long*)((char*)pr->hout + 64);
+  pr->counts = {(long long)hc[0], (long long)hc[1], (long long)hc[2], (long long)hc[3]};
+  // get_porosity (geometry.cc:335-364): fluid count / interior voxel count
+  if (p->porosity == -1.0) {
+    double vox = (double)((long long)g.nx * g.ny * g.nz);
+    pr->phi = (double)pr->counts.fluid / vox;
+  } else {
+    pr->phi = p->porosity;
+  }
+#undef CKF
+  *out = pr;
+  return PM_OK;
+}
+
+pm_status pm_problem_destroy(pm_problem* pr) {
+  if (!pr) return PM_OK;
+  if (pr->st) cudaStreamSynchronize(pr->st);
+  cudaFree(pr->codes_base);
+  cudaFree(pr->list);
+  cudaFree(pr->f64_base[0]);
+  cudaFree(pr->f64_base[1]);
+  cudaFree(pr->f32_base);
+  cudaFree(pr->partials);
+  cudaFree(pr->dout);
+  if (pr->hout) cudaFreeHost(pr->hout);
+  cudaFree(pr->scratch);
+  if (pr->ev0) cudaEventDestroy(pr->ev0);
+  if (pr->ev1) cudaEventDestroy(pr->ev1);
+  if (pr->st) cudaStreamDestroy(pr->st);
+  delete pr;
+  return PM_OK;
+}
+
+pm_status pm_iterate(pm_problem* pr, int n) {
+  if (!pr || n < 0) return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s = iterate_n(pr, n);
+  if (s != PM_OK) return s;
+  return device_sync(pr, "pm_iterate");
+}
+
+pm_status pm_compute_convergence(pm_problem* pr, double* permeability, double* conv) {
+  if (!pr || !permeability || !conv) return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s = reduce(pr, 0);
+  if (s != PM_OK) return s;
+  convergence_from(pr, pr->hout[2], permeability, conv);
+  return PM_OK;
+}
+
+pm_status pm_compute_permeability(pm_problem* pr, pm_result* res) {
+  if (!pr || !res) return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s = reduce(pr, 1);
+  if (s != PM_OK) return s;
+  permeability_from(pr, pr->hout, res);
+  return PM_OK;
+}
+
+pm_status pm_get_porosity(pm_problem* pr, double* porosity) {
+  if (!pr || !porosity) return set_error(PM_ERR_INVALID, "bad arguments");
+  *porosity = pr->phi;
+  return PM_OK;
+}
+
+pm_status pm_get_iteration(pm_problem* pr, int* iteration) {
+  if (!pr || !iteration) return set_error(PM_ERR_INVALID, "bad arguments");
+  *iteration = pr->iteration;
+  return PM_OK;
+}
+
+// calc_flow (calc_flow.cc:53-169)
+pm_status pm_solve(pm_problem* pr, pm_result* res) {
+  if (!pr || !res) return set_error(PM_ERR_INVALID, "bad arguments");
+  auto t0 = std::chrono::steady_clock::now();
+  const pm_params& p = pr->prm;
+  memset(res, 0, sizeof(*res));
+  double conv = pr->conv_valid ? pr->conv : 1.0 + p.eps;
+  double perm = pr->perm_prev;
+  pm_status s = PM_OK;
+  float block_ms = 0.f;
+  while (pr->iteration < p.max_iter && conv >= p.eps) {
+    // the next iteration at which the reference evaluates convergence
+    long long it = pr->iteration;
+    long long nxt = it;
+    if (nxt <= 1000) nxt = 1001;
+    nxt = ((nxt + p.it_eval - 1) / p.it_eval) * p.it_eval;
+    long long last = nxt < p.max_iter ? nxt : (long long)p.max_iter - 1;
+    int n = (int)(last - it + 1);
+    CK(cudaEventRecord(pr->ev0, pr->st));
+    if ((s = iterate_n(pr, n)) != PM_OK) return s;
+    CK(cudaEventRecord(pr->ev1, pr->st));
+    if ((s = device_sync(pr, "sweep block")) != PM_OK) return s;
+    CK(cudaEventElapsedTime(&block_ms, pr->ev0, pr->ev1));
+    pr->device_ms += block_ms;
+    if (last == nxt) {
+      if ((s = reduce(pr, 0)) != PM_OK) return s;
+      convergence_from(pr, pr->hout[2], &perm, &conv);
+      res->iterations = (int)last;
+      if (last % p.it_write == 0) {
+        if ((s = pm_compute_permeability(pr, res)) != PM_OK) return s;
+        if (p.write_log && p.log_file_name[0]) {
+          double tps = block_ms > 0 ? 1000.0 * n / block_ms : 0.0;
+          if ((s = write_log_row(p.log_file_name, pr->first_log, (int)last, conv, tps, *res)) !=
+              PM_OK)
+            return s;
+        }
+        pr->first_log = false;
+      }
+    }
+  }
+  pr->conv = conv;
+  pr->conv_valid = true;
+  pr->perm_prev = perm;
+  pm_result keep = *res;
+  if ((s = pm_compute_permeability(pr, res)) != PM_OK) return s;
+  res->iterations = keep.iterations;
+  res->sweeps = (int)pr->sweeps_done;
+  res->conv = conv;
+  res->converged = conv < p.eps;
+  res->permeability = perm;
+  res->device_ms = pr->device_ms;
+  res->wall_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  res->glups = pr->device_ms > 0 ? (double)pr->g.nvox * pr->sweeps_done / (pr->device_ms * 1e6)
+                                 : 0.0;
+  if (!isfinite(res->wk33) || !isfinite(perm))
+    return set_error(PM_ERR_NONFINITE, "non-finite permeability (conv=%g)", conv);
+  return PM_OK;
+}
+
+pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double* p) {
+  if (!pr) return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s;
+  if ((s = dc_flush(pr)) != PM_OK) return s;
+  double* out[4] = {u, v, w, p};
+  const Fields<double>& f = pr->F[pr->cur];
+  const double* src[4] = {f.u, f.v, f.w, f.p};
+  for (int k = 0; k < 4; ++k) {
+    if (!out[k]) continue;
+    CK(launch_pack64(src[k], nullptr, pr->codes, k == 3 && pr->order != PM_ORDER_REFERENCE, pr->g,
+                     (double*)pr->scratch, pr->st));
+    CK(cudaMemcpyAsync(out[k], pr->scratch, sizeof(double) * pr->g.nvox, cudaMemcpyDeviceToHost,
+                       pr->st));
+    if ((s = device_sync(pr, "pm_get_fields")) != PM_OK) return s;
+  }
+  return PM_OK;
+}
+
+pm_status pm_get_neighborhood(pm_problem* pr, int32_t* out) {
+  if (!pr || !out) return set_error(PM_ERR_INVALID, "bad arguments");
+  CK(launch_pack_codes(pr->codes, pr->g, (int*)pr->scratch, pr->st));
+  CK(cudaMemcpyAsync(out, pr->scratch, sizeof(int32_t) * pr->g.nvox, cudaMemcpyDeviceToHost,
+                     pr->st));
+  return device_sync(pr, "pm_get_neighborhood");
+}
+
+}  // extern "C"
+
+namespace pm {
+const pm_params* problem_params(const pm_problem* pr) { return &pr->prm; }
+long long problem_nvox(const pm_problem* pr) { return pr->g.nvox; }
+cudaStream_t problem_stream(const pm_problem* pr) { return pr->st; }
+}  // namespace pm

@@ -1,0 +1,114 @@
+// Internal declarations shared by the CUDA kernels and the host runtime of
+// poremaps_gb300.  Not part of the public C ABI (include/poremaps.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pm {
+
+// Physics constants of the reference (src/constants.h:46-64).
+constexpr double kOmega = 1.2;
+constexpr double kRe = 0.01;
+constexpr double kC2 = 1.5e6;
+constexpr double kDt = 1.0e-4;
+
+// Padded device layout.  A field element (x, y, z) of the padded domain
+// (x in [0, NX), NX = nx + 4, halo 2 on each side as in the reference) lives at
+// f[(z * NY + y) * px + x], where f points XOFF elements past the 256-byte
+// aligned allocation so that the first interior column x = 2 starts on a
+// 128-byte boundary; px (row pitch) is a multiple of 128 bytes.
+constexpr int kXoff64 = 14;
+constexpr int kXoff32 = 30;
+constexpr int kXoffC = 14;
+
+struct Grid {
+  int nx, ny, nz;
+  int NX, NY, NZ;
+  int per[3];          // periodic axes (x, y, z) from boundary_method
+  int px64, px32, pxc; // row pitches in elements
+  long long pl64, pl32, plc; // plane strides in elements
+  long long alloc64, alloc32, allocc; // elements to allocate (including XOFF)
+  long long nvox;      // nx*ny*nz
+};
+
+Grid make_grid(int nx, int ny, int nz, int boundary_method);
+
+template <typename T>
+struct Fields {
+  T* u;
+  T* v;
+  T* w;
+  T* p;
+};
+
+// Voxel code byte: 0 solid; 1..216 interior fluid with neighbourhood cases
+// (cx, cy, cz) in 1..6 as 1 + (cx-1)*36 + (cy-1)*6 + (cz-1); 255 fluid halo.
+constexpr uint8_t kHaloFluid = 255;
+
+// Reduction partials: fixed grid so the summation order never changes.
+constexpr int kRedBlocks = 592;  // 4 x 148; fixed independent of the device
+constexpr int kRedThreads = 256;
+constexpr int kRedVals = 9;      // sum u, v, w, max w, box u, v, w, p(zmin), p(zmax)
+
+struct Counts {
+  long long fluid;       // interior fluid voxels
+  long long box_fluid;   // fluid voxels inside dom_interest
+  long long p0_fluid;    // fluid voxels on the dom_interest zmin plane
+  long long pend_fluid;  // fluid voxels on the dom_interest zmax plane
+};
+
+// ---------------------------------------------------------------- launchers
+// All launchers are asynchronous on `st` and return the launch error.
+cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st);
+cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
+                              cudaStream_t st);
+cudaError_t launch_counts(const uint8_t* codes, const Grid& g, const int di[6],
+                          unsigned long long* out4, cudaStream_t st);
+cudaError_t launch_init64(Fields<double> f, const uint8_t* codes, const Grid& g,
+                          cudaStream_t st);
+cudaError_t launch_copy_fields64(Fields<double> dst, Fields<double> src, const Grid& g,
+                                 cudaStream_t st);
+cudaError_t launch_halo64(Fields<double> f, const Grid& g, cudaStream_t st);
+cudaError_t launch_reapply64(double* p, const uint8_t* codes, const Grid& g, cudaStream_t st);
+
+// Reference order: in-place lexicographic sweep as an exact hyperplane
+// wavefront, then halo exchange and reapply, n_iter times (cooperative launch).
+cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid& g,
+                             int solver, int n_iter, int* coop_blocks, cudaStream_t st);
+
+// Ping-pong Jacobi (phase 0) and red (1) / black (2) half-sweeps from A into B
+// over the fluid list; periodic halo copies and the pressure reapply fused.
+cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* codes,
+                           const int* list, int nlist, const Grid& g, int solver, int exact,
+                           int phase, cudaStream_t st);
+
+// Mixed precision (defect correction).  x: FP64 state, e: FP32 correction
+// (ping-pong), r: FP32 residual.
+cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
+                              cudaStream_t st);
+cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> e,
+                               const uint8_t* codes, const int* list, int nlist,
+                               const Grid& g, int solver, cudaStream_t st);
+cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
+                            const uint8_t* codes, const int* list, int nlist, const Grid& g,
+                            int solver, cudaStream_t st);
+cudaError_t launch_zero32(Fields<float> e, const Grid& g, cudaStream_t st);
+
+// Reductions.  mode 0: FP64 fields; mode 1: FP64 x + FP32 e.  full = 0 only
+// sums w.  partials: kRedBlocks*kRedVals doubles; out: kRedVals doubles.
+// implied3: the state stores swept pressure on the last interior plane and the
+// reapplied 3 is implied there (out-of-place orderings).
+cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full, int implied3,
+                          const uint8_t* codes, const Grid& g, const int di[6],
+                          double* partials, double* out, cudaStream_t st);
+
+cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
+                          const Grid& g, double* out, cudaStream_t st);
+cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st);
+
+// z-march TMA kernel for the FP32 correction sweep (dense tiles).
+struct ZmarchPlan;
+int zmarch_available();
+
+}  // namespace pm

@@ -1,0 +1,601 @@
+// Set-up, boundary, reduction and exact-arithmetic sweep kernels.
+// This translation unit is compiled with -fmad=false so that every
+// floating-point expression rounds exactly as the reference CPU program's
+// (which is built for x86-64 without FMA contraction).
+#include <cooperative_groups.h>
+
+#include "pm_internal.h"
+#include "pm_stencil.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pm {
+
+Grid make_grid(int nx, int ny, int nz, int bm) {
+  Grid g;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.NX = nx + 4; g.NY = ny + 4; g.NZ = nz + 4;
+  // main_stokes_solver.cc:163-165: periods from boundary_method
+  g.per[0] = g.per[1] = (bm == 0);
+  g.per[2] = (bm <= 2);
+  auto up = [](long long a, long long b) { return (a + b - 1) / b * b; };
+  g.px64 = (int)up(kXoff64 + g.NX, 16);
+  g.px32 = (int)up(kXoff32 + g.NX, 32);
+  g.pxc = (int)up(kXoffC + g.NX, 16);
+  g.pl64 = (long long)g.px64 * g.NY;
+  g.pl32 = (long long)g.px32 * g.NY;
+  g.plc = (long long)g.pxc * g.NY;
+  g.alloc64 = g.pl64 * g.NZ + 64;
+  g.alloc32 = g.pl32 * g.NZ + 64;
+  g.allocc = g.plc * g.NZ + 256;
+  g.nvox = (long long)nx * ny * nz;
+  return g;
+}
+
+// ------------------------------------------------------------------ geometry
+// Fluid status of padded voxel (x, y, z): interior from the raw file, halo
+// coordinates on periodic axes wrap (communicate_geom_halos with the rank as
+// its own neighbour), on non-periodic axes the halo is fluid (geometry halos
+// start at 0 and are never received, geometry.cc:98-106).
+__device__ __forceinline__ bool raw_solid(const uint8_t* raw, const Grid& g, int x, int y, int z) {
+  auto fold = [](int c, int n, int per, bool& outside) {
+    int i = c - 2;
+    if (i < 0 || i >= n) {
+      if (!per) { outside = true; return 0; }
+      i = i < 0 ? i + n : i - n;
+    }
+    return i;
+  };
+  bool outside = false;
+  int i = fold(x, g.nx, g.per[0], outside);
+  int j = fold(y, g.ny, g.per[1], outside);
+  int k = fold(z, g.nz, g.per[2], outside);
+  if (outside) return false;
+  return raw[((long long)k * g.ny + j) * g.nx + i] != 0;
+}
+
+// eval_geometry (geometry.cc:174-302) for every padded voxel.
+__global__ void k_codes(const uint8_t* raw, uint8_t* codes, Grid g) {
+  long long n = (long long)g.NX * g.NY * g.NZ;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.NX);
+    long long r = q / g.NX;
+    int y = (int)(r % g.NY);
+    int z = (int)(r / g.NY);
+    uint8_t code;
+    if (raw_solid(raw, g, x, y, z)) {
+      code = 0;
+    } else if (x < 2 || y < 2 || z < 2 || x >= g.NX - 2 || y >= g.NY - 2 || z >= g.NZ - 2) {
+      code = kHaloFluid;
+    } else {
+      int cs[3];
+      for (int d = 0; d < 3; ++d) {
+        int dx = d == 0, dy = d == 1, dz = d == 2;
+        bool l = raw_solid(raw, g, x - dx, y - dy, z - dz);
+        bool r = raw_solid(raw, g, x + dx, y + dy, z + dz);
+        int c;
+        if (l && r) c = 1;
+        else if (l && !r) c = raw_solid(raw, g, x + 2 * dx, y + 2 * dy, z + 2 * dz) ? 2 : 4;
+        else if (!l && r) c = raw_solid(raw, g, x - 2 * dx, y - 2 * dy, z - 2 * dz) ? 3 : 5;
+        else c = 6;
+        cs[d] = c;
+      }
+      code = (uint8_t)(1 + (cs[0] - 1) * 36 + (cs[1] - 1) * 6 + (cs[2] - 1));
+    }
+    codes[((long long)z * g.NY + y) * g.pxc + x] = code;
+  }
+}
+
+cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st) {
+  k_codes<<<1184, 256, 0, st>>>(raw, codes, g);
+  return cudaGetLastError();
+}
+
+// Interior fluid voxels in lexicographic order (x fastest) as linear interior
+// indices; built once, used by the sweep kernels so that warps only carry
+// fluid voxels.  Order: one block per (y, z) row with a ballot scan.
+__global__ void k_row_counts(const uint8_t* codes, Grid g, int* row_count) {
+  int row = blockIdx.x;  // z' * ny + y'
+  int yp = row % g.ny, zp = row / g.ny;
+  const uint8_t* c = codes + ((long long)(zp + 2) * g.NY + (yp + 2)) * g.pxc + 2;
+  int cnt = 0;
+  for (int x = threadIdx.x; x < g.nx; x += blockDim.x) cnt += c[x] != 0;
+  __shared__ int s[32];
+  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+    row_count[row] = t;
+  }
+}
+
+__global__ void k_row_fill(const uint8_t* codes, Grid g, const int* row_off, int* list) {
+  int row = blockIdx.x;
+  int yp = row % g.ny, zp = row / g.ny;
+  const uint8_t* c = codes + ((long long)(zp + 2) * g.NY + (yp + 2)) * g.pxc + 2;
+  __shared__ int base;
+  if (threadIdx.x == 0) base = row_off[row];
+  __syncthreads();
+  int lane = threadIdx.x & 31;
+  for (int x0 = 0; x0 < g.nx; x0 += 32) {
+    // one warp walks the row in order (deterministic, lexicographic)
+    if (threadIdx.x < 32) {
+      int x = x0 + lane;
+      bool f = x < g.nx && c[x] != 0;
+      unsigned m = __ballot_sync(0xffffffffu, f);
+      if (f) list[base + __popc(m & ((1u << lane) - 1))] = (int)(((long long)zp * g.ny + yp) * g.nx + x);
+      if (lane == 0) base += __popc(m);
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void k_scan_rows(const int* row_count, int nrows, int* row_off, int* total) {
+  // single block, sequential chunks (set-up only)
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int b = 0; b < nrows; b += blockDim.x) {
+    int i = b + threadIdx.x;
+    int v = i < nrows ? row_count[i] : 0;
+    // block inclusive scan
+    __shared__ int s[1024];
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+      int t = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nrows) row_off[i] = carry + s[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += s[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
+                              cudaStream_t st) {
+  int nrows = g.ny * g.nz;
+  int* tmp = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&tmp, sizeof(int) * 2 * (size_t)nrows, st);
+  if (e != cudaSuccess) return e;
+  k_row_counts<<<nrows, 128, 0, st>>>(codes, g, tmp);
+  k_scan_rows<<<1, 1024, 0, st>>>(tmp, nrows, tmp + nrows, count);
+  k_row_fill<<<nrows, 32, 0, st>>>(codes, g, tmp + nrows, list);
+  e = cudaGetLastError();
+  cudaFreeAsync(tmp, st);
+  return e;
+}
+
+// Fluid counts for the reductions (integers, deterministic).
+__global__ void k_counts(const uint8_t* codes, Grid g, int d0, int d1, int d2, int d3, int d4,
+                         int d5, unsigned long long* out) {
+  unsigned long long c[4] = {0, 0, 0, 0};
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.nx);
+    long long r = q / g.nx;
+    int y = (int)(r % g.ny);
+    int z = (int)(r / g.ny);
+    if (codes[((long long)(z + 2) * g.NY + (y + 2)) * g.pxc + (x + 2)] == 0) continue;
+    c[0]++;
+    if (x < d0 || x > d1 || y < d2 || y > d3 || z < d4 || z > d5) continue;
+    c[1]++;
+    if (z == d4) c[2]++;
+    if (z == d5) c[3]++;
+  }
+  for (int i = 0; i < 4; ++i) {
+    unsigned long long v = c[i];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(out + i, v);
+  }
+}
+
+cudaError_t launch_counts(const uint8_t* codes, const Grid& g, const int di[6],
+                          unsigned long long* out4, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out4, 0, 4 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  k_counts<<<592, 256, 0, st>>>(codes, g, di[0], di[1], di[2], di[3], di[4], di[5], out4);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ fields
+__device__ __forceinline__ bool is_halo(const Grid& g, int x, int y, int z) {
+  return x < 2 || y < 2 || z < 2 || x >= g.NX - 2 || y >= g.NY - 2 || z >= g.NZ - 2;
+}
+
+// allocate_initial_field (initialize.cc:69-121) + the pressure halo exchange
+// + set_halos_initial + the iteration-0 reapply_pressure_gradient
+// (calc_flow.cc:105-108), evaluated point-wise.
+__global__ void k_init64(Fields<double> f, const uint8_t* codes, Grid g) {
+  long long n = (long long)g.NX * g.NY * g.NZ;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.NX);
+    long long r = q / g.NX;
+    int y = (int)(r % g.NY);
+    int z = (int)(r / g.NY);
+    long long c = ((long long)z * g.NY + y) * g.px64 + x;
+    f.u[c] = 0.0;
+    f.v[c] = 0.0;
+    f.w[c] = 0.0;
+    // source voxel of the pressure value after the X, Y, Z halo exchange
+    int sx = x, sy = y, sz = z;
+    bool minus1 = false;
+    auto fold = [&](int& s, int n, int per) {
+      if (s < 2 || s >= n + 2) {
+        if (!per) minus1 = true;
+        else s = s < 2 ? s + n : s - n;
+      }
+    };
+    fold(sx, g.nx, g.per[0]);
+    fold(sy, g.ny, g.per[1]);
+    fold(sz, g.nz, g.per[2]);
+    double p;
+    if (minus1) {
+      p = -1.0;
+    } else {
+      bool fl = codes[((long long)sz * g.NY + sy) * g.pxc + sx] != 0;
+      p = fl ? (double)((g.nz - sz) + 2 + 2) : 0.0;
+    }
+    // reapply_pressure_gradient (boundary_conditions.cc:46-79) on planes 1,
+    // NZ-2 and NZ-3 for interior (x, y), where the geometry is fluid
+    bool ixy = x >= 2 && x < g.NX - 2 && y >= 2 && y < g.NY - 2;
+    bool fluid_here = codes[((long long)z * g.NY + y) * g.pxc + x] != 0;
+    if (ixy && fluid_here) {
+      if (z == 1) p = (double)(g.nz + 2);
+      if (z == g.NZ - 2) p = 2.0;
+      if (z == g.NZ - 3) p = 3.0;
+    }
+    f.p[c] = p;
+  }
+}
+
+cudaError_t launch_init64(Fields<double> f, const uint8_t* codes, const Grid& g,
+                          cudaStream_t st) {
+  k_init64<<<1184, 256, 0, st>>>(f, codes, g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_fields64(Fields<double> dst, Fields<double> src, const Grid& g,
+                                 cudaStream_t st) {
+  size_t bytes = sizeof(double) * (size_t)g.pl64 * g.NZ;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(dst.u, src.u, bytes, cudaMemcpyDeviceToDevice, st))) return e;
+  if ((e = cudaMemcpyAsync(dst.v, src.v, bytes, cudaMemcpyDeviceToDevice, st))) return e;
+  if ((e = cudaMemcpyAsync(dst.w, src.w, bytes, cudaMemcpyDeviceToDevice, st))) return e;
+  return cudaMemcpyAsync(dst.p, src.p, bytes, cudaMemcpyDeviceToDevice, st);
+}
+
+// communicate_halos (parallelization.cc:193-318) on one rank: periodic axes
+// copy the 2-deep faces from the opposite interior side; non-periodic halos
+// are left untouched.  Only face halos at interior positions of the other
+// two axes are ever read by the sweep, so those are the ones refreshed.
+template <typename T>
+__device__ __forceinline__ void halo_point(Fields<T> f, const Grid& g, long long px, long long pl,
+                                           long long q) {
+  // q enumerates 3 axes x 4 halo layers x (interior extent of the other two)
+  long long nyz = (long long)g.ny * g.nz, nxz = (long long)g.nx * g.nz,
+            nxy = (long long)g.nx * g.ny;
+  int ax;
+  long long r;
+  if (q < 4 * nyz) { ax = 0; r = q; }
+  else if (q < 4 * (nyz + nxz)) { ax = 1; r = q - 4 * nyz; }
+  else { ax = 2; r = q - 4 * (nyz + nxz); }
+  if (!g.per[ax]) return;
+  int layer = (int)(r & 3);
+  r >>= 2;
+  int x, y, z, sx, sy, sz;
+  // layer 0,1 -> halo 0,1 from interior n, n+1; layer 2,3 -> halo n+2, n+3 from 2, 3
+  if (ax == 0) {
+    y = (int)(r % g.ny) + 2; z = (int)(r / g.ny) + 2;
+    x = layer < 2 ? layer : g.nx + layer;
+    sx = layer < 2 ? g.nx + layer : layer;
+    sy = y; sz = z;
+  } else if (ax == 1) {
+    x = (int)(r % g.nx) + 2; z = (int)(r / g.nx) + 2;
+    y = layer < 2 ? layer : g.ny + layer;
+    sy = layer < 2 ? g.ny + layer : layer;
+    sx = x; sz = z;
+  } else {
+    x = (int)(r % g.nx) + 2; y = (int)(r / g.nx) + 2;
+    z = layer < 2 ? layer : g.nz + layer;
+    sz = layer < 2 ? g.nz + layer : layer;
+    sx = x; sy = y;
+  }
+  long long d = (long long)z * pl + (long long)y * px + x;
+  long long s = (long long)sz * pl + (long long)sy * px + sx;
+  f.u[d] = f.u[s];
+  f.v[d] = f.v[s];
+  f.w[d] = f.w[s];
+  f.p[d] = f.p[s];
+  (void)nxy;
+}
+
+__global__ void k_halo64(Fields<double> f, Grid g) {
+  long long n = 4LL * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    halo_point<double>(f, g, g.px64, g.pl64, q);
+}
+
+cudaError_t launch_halo64(Fields<double> f, const Grid& g, cudaStream_t st) {
+  k_halo64<<<592, 256, 0, st>>>(f, g);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ void reapply_point(double* p, const uint8_t* codes, const Grid& g,
+                                              long long q) {
+  int x = (int)(q % g.nx) + 2, y = (int)(q / g.nx) + 2;
+  long long c1 = ((long long)1 * g.NY + y), c2 = ((long long)(g.NZ - 2) * g.NY + y),
+            c3 = ((long long)(g.NZ - 3) * g.NY + y);
+  if (codes[c1 * g.pxc + x]) p[c1 * g.px64 + x] = (double)(g.nz + 2);
+  if (codes[c2 * g.pxc + x]) p[c2 * g.px64 + x] = 2.0;
+  if (codes[c3 * g.pxc + x]) p[c3 * g.px64 + x] = 3.0;
+}
+
+__global__ void k_reapply64(double* p, const uint8_t* codes, Grid g) {
+  long long n = (long long)g.nx * g.ny;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    reapply_point(p, codes, g, q);
+}
+
+cudaError_t launch_reapply64(double* p, const uint8_t* codes, const Grid& g, cudaStream_t st) {
+  k_reapply64<<<148, 256, 0, st>>>(p, codes, g);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ reference order
+template <int SOLVER>
+__global__ void __launch_bounds__(256) k_wavefront(Fields<double> f, const uint8_t* codes, Grid g,
+                                                   int n_iter) {
+  cg::grid_group grid = cg::this_grid();
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  const long long px = g.px64, pl = g.pl64;
+  const int T = g.nx + g.ny + g.nz - 2;
+  const long long nhalo =
+      4LL * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
+  for (int it = 0; it < n_iter; ++it) {
+    // central_diff5's lexicographic in-place order is reproduced exactly by
+    // hyperplanes t = x'+y'+z': every read at offsets -1/-2 lies on t-1/t-2
+    // (already updated), every read at +1/+2 on t+1/t+2 (not yet updated).
+    for (int t = 0; t < T; ++t) {
+      int zlo = max(0, t - (g.nx - 1) - (g.ny - 1)), zhi = min(g.nz - 1, t);
+      long long npairs = (long long)(zhi - zlo + 1) * g.ny;
+      for (long long q = tid; q < npairs; q += nth) {
+        int zp = zlo + (int)(q / g.ny), yp = (int)(q % g.ny);
+        int xp = t - zp - yp;
+        if (xp < 0 || xp >= g.nx) continue;
+        int x = xp + 2, y = yp + 2, z = zp + 2;
+        int code = codes[((long long)z * g.NY + y) * g.pxc + x];
+        if (!code) continue;
+        long long c = (long long)z * pl + (long long)y * px + x;
+        Stencil<double> s;
+        gather<double, 0, false, 0>(s, f, f, c, x, y, z, g, px, pl);
+        double un, vn, wn, pn;
+        update_exact<SOLVER>(s, code, un, vn, wn, pn);
+        f.u[c] = un;
+        f.v[c] = vn;
+        f.w[c] = wn;
+        f.p[c] = pn;
+      }
+      grid.sync();
+    }
+    for (long long q = tid; q < nhalo; q += nth) halo_point<double>(f, g, px, pl, q);
+    grid.sync();
+    for (long long q = tid; q < (long long)g.nx * g.ny; q += nth) reapply_point(f.p, codes, g, q);
+    grid.sync();
+  }
+}
+
+cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid& g, int solver,
+                             int n_iter, int* coop_blocks, cudaStream_t st) {
+  void* fn = solver == 1 ? (void*)k_wavefront<1> : solver == 2 ? (void*)k_wavefront<2>
+                                                               : (void*)k_wavefront<3>;
+  if (*coop_blocks <= 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    if (e != cudaSuccess) return e;
+    long long want = ((long long)g.ny * g.nz + 255) / 256;  // enough for one hyperplane
+    long long maxb = (long long)sms * (per > 0 ? per : 1);
+    *coop_blocks = (int)(want < maxb ? (want < 1 ? 1 : want) : maxb);
+  }
+  Fields<double> ff = f;
+  const uint8_t* cc = codes;
+  Grid gg = g;
+  int n = n_iter;
+  void* args[] = {&ff, &cc, &gg, &n};
+  return cudaLaunchCooperativeKernel(fn, dim3(*coop_blocks), dim3(256), args, 0, st);
+}
+
+// ------------------------------------------------------------------ FP64 sweeps (exact)
+template <int SOLVER, int PHASE>
+__global__ void __launch_bounds__(256) k_sweep64_exact(Fields<double> A, Fields<double> B,
+                                                       const uint8_t* codes, const int* list,
+                                                       int nlist, Grid g) {
+  const long long px = g.px64, pl = g.pl64;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
+    int lin = list[q];
+    int xp = lin % g.nx;
+    int r = lin / g.nx;
+    int yp = r % g.ny, zp = r / g.ny;
+    if (PHASE && (((xp + yp + zp) & 1) != PHASE - 1)) continue;
+    int x = xp + 2, y = yp + 2, z = zp + 2;
+    int code = codes[((long long)z * g.NY + y) * g.pxc + x];
+    long long c = (long long)z * pl + (long long)y * px + x;
+    Stencil<double> s;
+    gather<double, PHASE>(s, A, B, c, x, y, z, g, px, pl);
+    double un, vn, wn, pn;
+    update_exact<SOLVER>(s, code, un, vn, wn, pn);
+    write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
+  }
+}
+
+template <int SOLVER>
+static cudaError_t sweep_exact_s(Fields<double> A, Fields<double> B, const uint8_t* codes,
+                                 const int* list, int nlist, const Grid& g, int phase,
+                                 cudaStream_t st) {
+  int blocks = (nlist + 255) / 256;
+  if (blocks < 1) return cudaSuccess;
+  if (phase == 0) k_sweep64_exact<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  else if (phase == 1) k_sweep64_exact<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  else k_sweep64_exact<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  return cudaGetLastError();
+}
+
+cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* codes,
+                          const int* list, int nlist, const Grid& g, int solver, int phase,
+                          cudaStream_t st) {
+  if (solver == 1) return sweep_exact_s<1>(A, B, codes, list, nlist, g, phase, st);
+  if (solver == 2) return sweep_exact_s<2>(A, B, codes, list, nlist, g, phase, st);
+  return sweep_exact_s<3>(A, B, codes, list, nlist, g, phase, st);
+}
+
+// ------------------------------------------------------------------ reductions
+// compute_convergence / compute_permeability sums (evaluation.cc:54-262) with
+// a fixed grid and a fixed combination tree (bitwise reproducible).
+template <int MODE>
+__global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, Fields<float> e,
+                                                        int full, int implied3,
+                                                        const uint8_t* codes, Grid g,
+                                                        int d0, int d1, int d2, int d3, int d4,
+                                                        int d5, double* partials) {
+  double acc[kRedVals];
+  for (int i = 0; i < kRedVals; ++i) acc[i] = 0.0;
+  const bool dofi = d0 | d1 | d2 | d3 | d4 | d5;
+  const long long stride = (long long)kRedBlocks * kRedThreads;
+  for (long long q = blockIdx.x * (long long)kRedThreads + threadIdx.x; q < g.nvox; q += stride) {
+    int xp = (int)(q % g.nx);
+    long long r = q / g.nx;
+    int yp = (int)(r % g.ny), zp = (int)(r / g.ny);
+    int X = xp + 2, Y = yp + 2, Z = zp + 2;
+    if (!codes[((long long)Z * g.NY + Y) * g.pxc + X]) continue;
+    long long c = (long long)Z * g.pl64 + (long long)Y * g.px64 + X;
+    long long c32 = (long long)Z * g.pl32 + (long long)Y * g.px32 + X;
+    double w = x.w[c];
+    if (MODE == 1) w += (double)e.w[c32];
+    acc[2] += w;
+    if (!full) continue;
+    double u = x.u[c], v = x.v[c];
+    if (MODE == 1) { u += (double)e.u[c32]; v += (double)e.v[c32]; }
+    acc[0] += u;
+    acc[1] += v;
+    if (w > acc[3]) acc[3] = w;
+    if (!dofi) continue;
+    if (xp < d0 || xp > d1 || yp < d2 || yp > d3 || zp < d4 || zp > d5) continue;
+    acc[4] += u;
+    acc[5] += v;
+    acc[6] += w;
+    double p = x.p[c];
+    if (MODE == 1) p += (double)e.p[c32];
+    if (implied3 && zp == g.nz - 1) p = 3.0;
+    if (zp == d4) acc[7] += p;
+    if (zp == d5) acc[8] += p;
+  }
+  __shared__ double sh[kRedVals][kRedThreads];
+  for (int i = 0; i < kRedVals; ++i) sh[i][threadIdx.x] = acc[i];
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < (unsigned)o)
+      for (int i = 0; i < kRedVals; ++i) {
+        double a = sh[i][threadIdx.x], b = sh[i][threadIdx.x + o];
+        sh[i][threadIdx.x] = (i == 3) ? (b > a ? b : a) : a + b;
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x < kRedVals) partials[blockIdx.x * kRedVals + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_reduce_final(const double* partials, double* out) {
+  // one block of 1024 threads, fixed tree over kRedBlocks partials
+  __shared__ double sh[1024];
+  for (int i = 0; i < kRedVals; ++i) {
+    double a = (threadIdx.x < (unsigned)kRedBlocks) ? partials[threadIdx.x * kRedVals + i] : 0.0;
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = 512; o > 0; o >>= 1) {
+      if (threadIdx.x < (unsigned)o) {
+        double x = sh[threadIdx.x], y = sh[threadIdx.x + o];
+        sh[threadIdx.x] = (i == 3) ? (y > x ? y : x) : x + y;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[i] = sh[0];
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full, int implied3,
+                          const uint8_t* codes, const Grid& g, const int di[6], double* partials,
+                          double* out, cudaStream_t st) {
+  if (mode == 0)
+    k_reduce<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
+                                                     di[2], di[3], di[4], di[5], partials);
+  else
+    k_reduce<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
+                                                     di[2], di[3], di[4], di[5], partials);
+  k_reduce_final<<<1, 1024, 0, st>>>(partials, out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ export
+// Interior of a padded FP64 field into a dense x-fastest array (the layout of
+// write_output_raw, output.cc:82-91), optionally plus an FP32 correction.
+// With implied3, fluid voxels of the last interior plane export the
+// reapplied pressure 3 (the out-of-place orderings store the swept value).
+__global__ void k_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
+                         Grid g, double* out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.nx);
+    long long r = q / g.nx;
+    int y = (int)(r % g.ny), z = (int)(r / g.ny);
+    double v = f[(long long)(z + 2) * g.pl64 + (long long)(y + 2) * g.px64 + x + 2];
+    if (e) v += (double)e[(long long)(z + 2) * g.pl32 + (long long)(y + 2) * g.px32 + x + 2];
+    if (implied3 && z == g.nz - 1 &&
+        codes[(long long)(z + 2) * g.plc + (long long)(y + 2) * g.pxc + x + 2])
+      v = 3.0;
+    out[q] = v;
+  }
+}
+
+cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
+                          const Grid& g, double* out, cudaStream_t st) {
+  k_pack64<<<1184, 256, 0, st>>>(f, e, codes, implied3, g, out);
+  return cudaGetLastError();
+}
+
+// Neighbourhood codes as the reference stores them: 100cx + 10cy + cz, -1 solid.
+__global__ void k_pack_codes(const uint8_t* codes, Grid g, int* out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.nx);
+    long long r = q / g.nx;
+    int y = (int)(r % g.ny), z = (int)(r / g.ny);
+    int c = codes[(long long)(z + 2) * g.plc + (long long)(y + 2) * g.pxc + x + 2];
+    int v = -1;
+    if (c) {
+      int cx, cy, cz;
+      decode_cases(c, cx, cy, cz);
+      v = 100 * cx + 10 * cy + cz;
+    }
+    out[q] = v;
+  }
+}
+
+cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st) {
+  k_pack_codes<<<1184, 256, 0, st>>>(codes, g, out);
+  return cudaGetLastError();
+}
+
+}  // namespace pm

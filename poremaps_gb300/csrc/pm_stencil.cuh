@@ -1,0 +1,256 @@
+// Per-voxel update of the pseudo-time Stokes sweep (the body of
+// central_diff5, src/solver.cc:136-220 of the reference) in two arithmetic
+// forms:
+//   * update_exact: the reference's operation order term by term (translation
+//     units that use it are compiled with -fmad=false), bit-identical to the
+//     reference CPU program;
+//   * update_fast: the same linear map regrouped into a coefficient form with
+//     FMAs (about 33 floating-point instructions per fluid voxel instead of
+//     ~70 plus three divisions), used by the FP64 fast sweeps and by the FP32
+//     correction sweeps of the mixed-precision form.
+#pragma once
+
+#include "pm_internal.h"
+
+namespace pm {
+
+// Values of the 4 fields a fluid voxel reads (axis-aligned offsets only).
+template <typename T>
+struct Stencil {
+  T uc, uxm, uxp, uym, uyp, uymm, uypp, uzm, uzp, uzmm, uzpp;
+  T vc, vxm, vxp, vxmm, vxpp, vym, vyp, vzm, vzp, vzmm, vzpp;
+  T wc, wxm, wxp, wxmm, wxpp, wym, wyp, wymm, wypp, wzm, wzp;
+  T pc, pxm, pym, pzm;
+};
+
+// code byte 1..216 -> neighbourhood cases (cx, cy, cz) in 1..6 (the
+// split_number of src/solver.cc:94-109 applied to 100cx + 10cy + cz).
+__device__ __forceinline__ void decode_cases(int code, int& cx, int& cy, int& cz) {
+  int c = code - 1;
+  int a = c / 36;
+  int rem = c - a * 36;
+  int b = rem / 6;
+  cx = a + 1;
+  cy = b + 1;
+  cz = rem - b * 6 + 1;
+}
+
+// The left neighbour along an axis is solid exactly for cases 1, 2 and 4 of
+// eval_geometry (src/geometry.cc:273-296).
+__device__ __forceinline__ bool left_solid(int cs) { return cs == 1 || cs == 2 || cs == 4; }
+
+// get_2nd_derivation, src/solver.cc:57-91, operand order preserved.
+__device__ __forceinline__ double d2_exact(int cs, double ll, double l, double m, double r,
+                                           double rr) {
+  double d = 0.0;
+  if (cs == 1) d = -8.0 * m;
+  else if (cs == 2) d = 8.0 / 3.0 * r - 16.0 / 3.0 * m;
+  else if (cs == 3) d = 8.0 / 3.0 * l - 16.0 / 3.0 * m;
+  else if (cs == 4) d = 2.0 * r - 5.0 * m - 1.0 / 5.0 * rr;
+  else if (cs == 5) d = 2.0 * l - 1.0 / 5.0 * ll - 5.0 * m;
+  else if (cs == 6) d = l - 2.0 * m + r;
+  return d;
+}
+
+// central_diff5 body (src/solver.cc:142-219) for one fluid voxel.
+template <int SOLVER>
+__device__ __forceinline__ void update_exact(const Stencil<double>& s, int code, double& un,
+                                             double& vn, double& wn, double& pn) {
+  int cx, cy, cz;
+  decode_cases(code, cx, cy, cz);
+  const bool lx = left_solid(cx), ly = left_solid(cy), lz = left_solid(cz);
+  double dp_dz = lz ? 0. : -s.pzm + s.pc;
+  double dp_dy = ly ? 0. : -s.pym + s.pc;
+  double dp_dx = lx ? 0. : -s.pxm + s.pc;
+  double uxx = (s.uxm - 2 * s.uc + s.uxp);
+  double vyy = (s.vym - 2 * s.vc + s.vyp);
+  double wzz = (s.wzm - 2 * s.wc + s.wzp);
+  double vxx = d2_exact(cx, s.vxmm, s.vxm, s.vc, s.vxp, s.vxpp);
+  double wxx = d2_exact(cx, s.wxmm, s.wxm, s.wc, s.wxp, s.wxpp);
+  double uyy = d2_exact(cy, s.uymm, s.uym, s.uc, s.uyp, s.uypp);
+  double wyy = d2_exact(cy, s.wymm, s.wym, s.wc, s.wyp, s.wypp);
+  double uzz = d2_exact(cz, s.uzmm, s.uzm, s.uc, s.uzp, s.uzpp);
+  double vzz = d2_exact(cz, s.vzmm, s.vzm, s.vc, s.vzp, s.vzpp);
+  double fu = uxx + uyy + uzz;
+  double fv = vyy + vzz + vxx;
+  double fw = wzz + wxx + wyy;
+  double v_sum = 0.0;
+  if (SOLVER == 1) v_sum = (s.wzp - s.wc + s.vyp - s.vc + s.uxp - s.uc);
+  if (SOLVER == 1 || SOLVER == 2) {
+    un = lx ? 0.0 : s.uc + (-dp_dx + fu / kRe) * kDt;
+    vn = ly ? 0.0 : s.vc + (-dp_dy + fv / kRe) * kDt;
+    wn = lz ? 0.0 : s.wc + (-dp_dz + fw / kRe) * kDt;
+  } else {
+    un = (1.0 - kOmega) * s.uc + kOmega * (-dp_dx + fu / kRe) * kDt;
+    vn = (1.0 - kOmega) * s.vc + kOmega * (-dp_dy + fv / kRe) * kDt;
+    wn = (1.0 - kOmega) * s.wc + kOmega * (-dp_dz + fw / kRe) * kDt;
+  }
+  if (SOLVER == 2 || SOLVER == 3) v_sum = (s.wzp - wn + s.vyp - vn + s.uxp - un);
+  pn = s.pc - kC2 * v_sum * kDt;
+}
+
+// Coefficient form.  Each wall-aware stencil of case cs is
+//   a(cs) * centre + cA(cs) * A + cB(cs) * B
+// with A, B the (at most two) off-centre points it uses.
+template <typename T>
+struct CaseCoef {
+  T a, cA, cB;
+};
+
+template <typename T>
+__device__ __forceinline__ CaseCoef<T> case_coef(int cs) {
+  CaseCoef<T> k;
+  switch (cs) {
+    case 1: k.a = T(-8.0); k.cA = T(0.0); k.cB = T(0.0); break;
+    case 2: k.a = T(-16.0 / 3.0); k.cA = T(8.0 / 3.0); k.cB = T(0.0); break;
+    case 3: k.a = T(-16.0 / 3.0); k.cA = T(8.0 / 3.0); k.cB = T(0.0); break;
+    case 4: k.a = T(-5.0); k.cA = T(2.0); k.cB = T(-0.2); break;
+    case 5: k.a = T(-5.0); k.cA = T(2.0); k.cB = T(-0.2); break;
+    default: k.a = T(-2.0); k.cA = T(1.0); k.cB = T(1.0); break;
+  }
+  return k;
+}
+
+// A = left for cases 3, 5, 6, else right; B = second right (4), second left
+// (5), right (6); unused (coefficient 0) otherwise.
+template <typename T>
+__device__ __forceinline__ void case_pick(int cs, T ll, T l, T r, T rr, T& A, T& B) {
+  A = (cs == 3 || cs == 5 || cs == 6) ? l : r;
+  B = cs == 4 ? rr : (cs == 5 ? ll : r);
+}
+
+// One velocity component: the along-axis 3-point term plus two cross-axis
+// wall stencils, the pressure difference, and the solver's relaxation.
+template <typename T, int SOLVER>
+__device__ __forceinline__ T vel_fast(T c, T am, T ap, int cs1, T ll1, T l1, T r1, T rr1, int cs2,
+                                      T ll2, T l2, T r2, T rr2, T dp, bool zero) {
+  const CaseCoef<T> k1 = case_coef<T>(cs1), k2 = case_coef<T>(cs2);
+  T A1, B1, A2, B2;
+  case_pick<T>(cs1, ll1, l1, r1, rr1, A1, B1);
+  case_pick<T>(cs2, ll2, l2, r2, rr2, A2, B2);
+  T f = am + ap;
+  f = fma(k1.cA, A1, f);
+  f = fma(k1.cB, B1, f);
+  f = fma(k2.cA, A2, f);
+  f = fma(k2.cB, B2, f);
+  f = fma(T(-2.0) + k1.a + k2.a, c, f);  // centre coefficient (exact small sums)
+  const T K = T(kDt / kRe);
+  if (SOLVER == 3) {
+    // (1 - w) c + w (-dp + f / Re) dt
+    T t = fma(T(kDt / kRe * kOmega), f, T(1.0 - kOmega) * c);
+    return fma(T(-kDt * kOmega), dp, t);
+  }
+  T t = fma(K, f, c);
+  t = fma(T(-kDt), dp, t);
+  return zero ? T(0.0) : t;
+}
+
+template <typename T, int SOLVER>
+__device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un, T& vn, T& wn,
+                                            T& pn) {
+  int cx, cy, cz;
+  decode_cases(code, cx, cy, cz);
+  const bool lx = left_solid(cx), ly = left_solid(cy), lz = left_solid(cz);
+  const T dpx = lx ? T(0) : s.pc - s.pxm;
+  const T dpy = ly ? T(0) : s.pc - s.pym;
+  const T dpz = lz ? T(0) : s.pc - s.pzm;
+  T div0 = T(0);
+  if (SOLVER == 1) div0 = ((s.wzp - s.wc) + (s.vyp - s.vc)) + (s.uxp - s.uc);
+  // u: along x, cross y (cy) and z (cz)
+  un = vel_fast<T, SOLVER>(s.uc, s.uxm, s.uxp, cy, s.uymm, s.uym, s.uyp, s.uypp, cz, s.uzmm,
+                           s.uzm, s.uzp, s.uzpp, dpx, lx);
+  // v: along y, cross x (cx) and z (cz)
+  vn = vel_fast<T, SOLVER>(s.vc, s.vym, s.vyp, cx, s.vxmm, s.vxm, s.vxp, s.vxpp, cz, s.vzmm,
+                           s.vzm, s.vzp, s.vzpp, dpy, ly);
+  // w: along z, cross x (cx) and y (cy)
+  wn = vel_fast<T, SOLVER>(s.wc, s.wzm, s.wzp, cx, s.wxmm, s.wxm, s.wxp, s.wxpp, cy, s.wymm,
+                           s.wym, s.wyp, s.wypp, dpz, lz);
+  T div = (SOLVER == 1) ? div0 : ((s.wzp - wn) + (s.vyp - vn)) + (s.uxp - un);
+  pn = fma(T(-kC2 * kDt), div, s.pc);
+}
+
+// Gather of the stencil values of one interior voxel.
+template <typename T>
+__device__ __forceinline__ T ldA(const T* p, bool nc) {
+  return nc ? __ldg(p) : __ldcg(p);
+}
+
+// P3 selects how the centre pressure of a voxel on the last interior plane
+// (z = NZ-3) is read.  The out-of-place orderings store the swept,
+// pre-reapply pressure there (their -x/-y neighbours on that plane must see it,
+// as in the reference's in-place order, boundary_conditions.cc:46-79 runs only
+// after the sweep) and imply the reapplied value 3 for the voxel itself:
+//   0: stored value (in-place reference order, explicit reapply)
+//   1: 3 (FP64 state)         2: 0 (homogeneous correction of the mixed form)
+template <typename T, int PHASE, bool NC = true, int P3 = 1>
+__device__ __forceinline__ void gather(Stencil<T>& s, const Fields<T>& A, const Fields<T>& B,
+                                       long long c, int x, int y, int z, const Grid& g,
+                                       long long px, long long pl) {
+  const long long sx = 1, sy = px, sz = pl;
+  // PHASE 2 (black): interior +-1 neighbours are red and already updated (in
+  // B); every other read (centre, +-2, halos) is the previous iterate (A).
+  auto P = [&](const T* a, const T* b, long long o, bool interior) -> T {
+    return (PHASE == 2 && interior) ? b[c + o] : ldA(a + c + o, NC);
+  };
+  const bool ixm = x - 1 >= 2, ixp = x + 1 <= g.NX - 3;
+  const bool iym = y - 1 >= 2, iyp = y + 1 <= g.NY - 3;
+  const bool izm = z - 1 >= 2, izp = z + 1 <= g.NZ - 3;
+  s.uc = ldA(A.u + c, NC);
+  s.vc = ldA(A.v + c, NC);
+  s.wc = ldA(A.w + c, NC);
+  s.pc = (P3 != 0 && z == g.NZ - 3) ? T(P3 == 1 ? 3.0 : 0.0) : ldA(A.p + c, NC);
+  s.uxm = P(A.u, B.u, -sx, ixm); s.uxp = P(A.u, B.u, sx, ixp);
+  s.uym = P(A.u, B.u, -sy, iym); s.uyp = P(A.u, B.u, sy, iyp);
+  s.uzm = P(A.u, B.u, -sz, izm); s.uzp = P(A.u, B.u, sz, izp);
+  s.uymm = ldA(A.u + c - 2 * sy, NC); s.uypp = ldA(A.u + c + 2 * sy, NC);
+  s.uzmm = ldA(A.u + c - 2 * sz, NC); s.uzpp = ldA(A.u + c + 2 * sz, NC);
+  s.vxm = P(A.v, B.v, -sx, ixm); s.vxp = P(A.v, B.v, sx, ixp);
+  s.vym = P(A.v, B.v, -sy, iym); s.vyp = P(A.v, B.v, sy, iyp);
+  s.vzm = P(A.v, B.v, -sz, izm); s.vzp = P(A.v, B.v, sz, izp);
+  s.vxmm = ldA(A.v + c - 2 * sx, NC); s.vxpp = ldA(A.v + c + 2 * sx, NC);
+  s.vzmm = ldA(A.v + c - 2 * sz, NC); s.vzpp = ldA(A.v + c + 2 * sz, NC);
+  s.wxm = P(A.w, B.w, -sx, ixm); s.wxp = P(A.w, B.w, sx, ixp);
+  s.wym = P(A.w, B.w, -sy, iym); s.wyp = P(A.w, B.w, sy, iyp);
+  s.wzm = P(A.w, B.w, -sz, izm); s.wzp = P(A.w, B.w, sz, izp);
+  s.wxmm = ldA(A.w + c - 2 * sx, NC); s.wxpp = ldA(A.w + c + 2 * sx, NC);
+  s.wymm = ldA(A.w + c - 2 * sy, NC); s.wypp = ldA(A.w + c + 2 * sy, NC);
+  s.pxm = P(A.p, B.p, -sx, ixm);
+  s.pym = P(A.p, B.p, -sy, iym);
+  s.pzm = P(A.p, B.p, -sz, izm);
+}
+
+// Write the new values of interior voxel (x, y, z) and, on periodic axes,
+// its halo copies (the halo exchange fused into the sweep).  The pressure
+// reapply is fused too: the z-halo copies on planes 1 and NZ-2 hold nz+2 and 2
+// (their geometry is this fluid voxel); x/y halo copies and the last interior
+// plane keep the swept, pre-reapply value, as the reference's
+// exchange-then-reapply order leaves the halos (the 3 of the last plane is
+// implied, see gather).  HOMOG (correction sweeps of the mixed form) writes 0
+// where the reapply writes a constant.
+template <typename T, bool HOMOG>
+__device__ __forceinline__ void write_voxel(const Fields<T>& B, long long c, int x, int y, int z,
+                                            const Grid& g, long long px, long long pl, T un,
+                                            T vn, T wn, T pn) {
+  const T pin = HOMOG ? T(0) : T(g.nz + 2), pout = HOMOG ? T(0) : T(2.0);
+  B.u[c] = un;
+  B.v[c] = vn;
+  B.w[c] = wn;
+  B.p[c] = pn;  // last interior plane: swept value stored, reapplied 3 implied
+  auto put = [&](long long o, T pv) {
+    B.u[c + o] = un; B.v[c + o] = vn; B.w[c + o] = wn; B.p[c + o] = pv;
+  };
+  if (g.per[0]) {
+    if (x < 4) put((long long)g.nx, pn);
+    if (x >= g.nx) put(-(long long)g.nx, pn);
+  }
+  if (g.per[1]) {
+    if (y < 4) put((long long)g.ny * px, pn);
+    if (y >= g.ny) put(-(long long)g.ny * px, pn);
+  }
+  if (g.per[2]) {
+    if (z < 4) put((long long)g.nz * pl, z == 2 ? pout : pn);
+    if (z >= g.nz) put(-(long long)g.nz * pl, z == g.nz + 1 ? pin : pn);
+  }
+}
+
+}  // namespace pm
