@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Benchmark of the POREMAPS pseudo-time Stokes sweep on GB300.
+
+Workload (default): a 128^3 periodic overlapping-sphere pack (radii U[4,10]
+voxels, solid fraction 0.65, z-percolating, seeded), voxel size 1e-5 m,
+boundary_method 0, SOR (solving_algorithm 3), eps 1e-6, full permeability
+tensor through the three axis-rotated problems.  One step = one it_eval block
+(100 sweeps + the convergence evaluation) on each of the three rotated
+problems, all resident in HBM.  Headline form: FP32 correction sweeps + FP64
+defect correction (mixed); the plain FP64 form is measured beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs N independent replicas (torchrun, one rank per GPU): the solver
+does not shard, so there is no data-path collective; the barrier and the
+max-over-ranks timing use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+SWEEPS_PER_BLOCK = 100
+ALGO_BYTES_MIXED_INNER = 48.125  # read e (4 x 4 B) + read r (4 x 4 B) + write e (4 x 4 B) + 1 bit
+ALGO_BYTES_FP64 = 64.125         # read 4 x 8 B + write 4 x 8 B + 1 bit
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
+                    help="run two it_eval blocks of one resident problem and exit (a small, "
+                         "self-contained case for ncu captures)")
+    return ap.parse_args()
+
+
+def workload(size: int):
+    from poremaps_gb300 import synth
+
+    g = synth.sphere_pack((size, size, size), rmin=4.0, rmax=10.0, solid_fraction=0.65,
+                          seed=2024)
+    # flow along z (as stored), along x (z' = x, y' = z, x' = y), along y (z' = y, y' = x, x' = z)
+    rots = [np.ascontiguousarray(g), np.ascontiguousarray(np.transpose(g, (2, 0, 1))),
+            np.ascontiguousarray(np.transpose(g, (1, 2, 0)))]
+    return g, rots
+
+
+def config_dict(size, g):
+    return {"workload": f"sphere-pack {size}^3 (radii U[4,10], solid 0.65, seed 2024), SOR, "
+                        "boundary_method 0, eps 1e-6, 3 axis-rotated problems (tensor)",
+            "size": [size, size, size], "porosity": round(float(1 - g.mean()), 6),
+            "solving_algorithm": 3, "boundary_method": 0, "voxel_size": 1e-5,
+            "sweeps_per_step": 3 * SWEEPS_PER_BLOCK, "order": "jacobi",
+            "l2": "256 MB buffer written between timed steps",
+            "parallelism": "replicas (one independent domain per GPU)"}
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            c = [x.strip() for x in ln.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax = max(smax, float(c[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU side
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def write_case(d, g, max_iter=100000001):
+    nz, ny, nx = g.shape
+    g.tofile(os.path.join(d, "geom.raw"))
+    with open(os.path.join(d, "in.inp"), "w") as f:
+        f.write(f"dom_decomposition 1 1 1\nboundary_method 0\ngeometry_file_name geom.raw\n"
+                f"size_x_y_z  {nx} {ny} {nz}\nvoxel_size  1e-05\nmax_iter    {max_iter}\n"
+                f"it_eval    100\nit_write   100\nlog_file_name run.log\nsolving_algorithm 3\n"
+                f"eps 1e-06\nporosity -1.0\ndom_interest 0 0 0 0 0 0\nwrite_output 0 0 0 0\n")
+
+
+def oracle_cli():
+    path = os.path.join(ROOT, "oracle", "_build", "oracle_cli")
+    if not os.path.exists(path):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True,
+                       stdout=subprocess.DEVNULL)
+    return path
+
+
+def cpu_run(g, sweeps: int, cores: int):
+    """The CPU restatement of the reference sweep (bitwise equal to the
+    reference program) on `cores` z-slabs, one thread each: the reference run
+    with dom_decomposition 1 1 cores."""
+    with tempfile.TemporaryDirectory() as d:
+        write_case(d, g)
+        r = subprocess.run([oracle_cli(), "in.inp", "--slabs", str(cores), "--threads",
+                            str(cores), "--sweeps", str(sweeps)], cwd=d, capture_output=True,
+                           text=True, check=True)
+        return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_cores(nz: int) -> int:
+    n = os.cpu_count() or 1
+    return max(1, min(n, nz // 2))
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    g, _ = workload(args.size)
+    cores = cpu_cores(g.shape[0])
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_run(g, SWEEPS_PER_BLOCK, cores)
+        if i >= args.warmup:
+            times.append(r["seconds"])
+    sec = statistics.mean(times)
+    glups = g.size * SWEEPS_PER_BLOCK / sec / 1e9
+    sample = (f"{SWEEPS_PER_BLOCK} sweeps of the unrotated {args.size}^3 problem per step "
+              f"(reference order, {cores} z-slabs)")
+    out = {"metric": "GLUP/s", "value": glups, "unit": "GLUP/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "impl": "reference", "config": config_dict(args.size, g),
+           "cpu_baseline": {"value": glups, "unit": "GLUP/s", "cores": cores, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": glups, "unit": "GLUP/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    out["config"]["sweeps_per_step"] = SWEEPS_PER_BLOCK
+    out["config"]["order"] = "reference (in-place lexicographic, per slab)"
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    import poremaps_gb300 as pm
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pm.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    g, rots = workload(args.size)
+    nvox = g.size
+    flush = torch.empty(256 * 2**20 // 4, dtype=torch.float32, device="cuda")
+    common = dict(solving_algorithm=3, boundary_method=0, voxel_size=1e-5, eps=1e-6,
+                  it_eval=SWEEPS_PER_BLOCK, it_write=SWEEPS_PER_BLOCK, order="jacobi")
+
+    def timed_form(precision: str, steps: int, warmup: int):
+        probs = [pm.Problem(r, None, precision=precision, **common) for r in rots]
+        perm = [0.0, 0.0, 0.0]
+        conv = [0.0, 0.0, 0.0]
+        for _ in range(warmup):
+            for i, p in enumerate(probs):
+                _, conv[i], perm[i] = p.block_timed(SWEEPS_PER_BLOCK, True, perm[i])
+        barrier()
+        launches0 = pm.kernel_launches()
+        total_ms = 0.0
+        with ClockSampler(local) as clk:
+            for _ in range(steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                for i, p in enumerate(probs):
+                    ms, conv[i], perm[i] = p.block_timed(SWEEPS_PER_BLOCK, True, perm[i])
+                    total_ms += ms
+            barrier()
+        launches = pm.kernel_launches() - launches0
+        ms_step = max_over_ranks(total_ms / steps)
+        return probs, perm, ms_step, launches, clk.summary()
+
+    # headline: mixed precision
+    probs_mx, perm_mx, ms_mx, launches_mx, clocks = timed_form("mixed", args.steps, args.warmup)
+    lups_step = 3 * SWEEPS_PER_BLOCK * nvox
+    value = world * lups_step / (ms_mx * 1e-3) / 1e9
+    kernel_ms = probs_mx[2].kernel_time(0, 50)
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = nvox * ALGO_BYTES_MIXED_INNER / (kernel_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_dc_inner_sphere128_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath))
+        traffic = t["dram_bytes_per_launch"] * nvox / t["nvox"]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "k_dc_inner (FP32 correction sweep)",
+                "algorithmic_bytes_per_lup": ALGO_BYTES_MIXED_INNER,
+                "kernel_ms": kernel_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst, of measured)" if peaks
+                               else "fallback 6.8 TB/s (of fallback)"}
+    forms = {"mixed": {"glups": value, "ms_per_step": ms_mx, "inner_kernel_ms": kernel_ms}}
+
+    k_rel = None
+    if not args.no_fp64:
+        probs_64, perm_64, ms_64, _, _ = timed_form("fp64", max(2, args.steps // 2),
+                                                    max(1, args.warmup))
+        k64 = probs_64[2].kernel_time(0, 10)
+        forms["fp64"] = {"glups": world * lups_step / (ms_64 * 1e-3) / 1e9, "ms_per_step": ms_64,
+                         "sweep_kernel_ms": k64,
+                         "hbm_frac_of_measured": nvox * ALGO_BYTES_FP64 / (k64 * 1e-3) / 1e9 / peak,
+                         "note": "FP64 sweeps are bound by the FP64 pipe of GB300, not by HBM"}
+        for p in probs_64:
+            p.close()
+    # k of the mixed form against the FP64 form after the same 1200 iterations
+    # (same ordering, same trajectory in exact arithmetic)
+    if not args.no_fp64:
+        ks = []
+        for prec in ("mixed", "fp64"):
+            with pm.Problem(rots[2], None, precision=prec, **common) as p:
+                p.iterate(1200)
+                ks.append(p.permeability())
+        k_rel = max(abs(getattr(ks[0], a) - getattr(ks[1], a)) for a in ("wk13", "wk23", "wk33")) \
+            / abs(ks[1].wk33)
+    res_mx = [p.permeability() for p in probs_mx]
+    for p in probs_mx:
+        p.close()
+
+    # end to end: the C-ABI tensor call from host geometry to host K
+    e2e_iters = 1200
+    e2e_times = []
+    for i in range(3):
+        barrier()
+        t0 = time.perf_counter()
+        K, res3 = pm.solve_tensor(g, None, max_iter=e2e_iters, precision="mixed", **common)
+        t1 = time.perf_counter()
+        if i >= 1:
+            e2e_times.append(t1 - t0)
+    e2e_s = max_over_ranks(statistics.mean(e2e_times))
+    checks = len([it for it in range(1001, e2e_iters) if it % SWEEPS_PER_BLOCK == 0])
+    e2e = {"value": world * 3 * e2e_iters * nvox / e2e_s / 1e9, "unit": "GLUP/s",
+           "h2d_bytes_per_step": 3 * nvox,
+           "d2h_bytes_per_step": 3 * (checks + 1) * 9 * 8 + 9 * 8,
+           "seconds_per_step": e2e_s,
+           "step": f"pm_solve_tensor, {e2e_iters} iterations per rotated problem, host geometry "
+                   "in, host tensor out"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = cpu_cores(g.shape[0])
+        sweeps = 200
+        r = cpu_run(g, sweeps, cores)
+        cpu = {"value": r["mlups"] / 1e3, "unit": "GLUP/s", "cores": cores, "kind": "port",
+               "sample": f"{sweeps} reference-order sweeps of the unrotated {args.size}^3 "
+                         f"problem on {cores} z-slab threads (oracle restatement, bitwise equal "
+                         f"to the reference program), {r['seconds']:.2f} s"}
+
+    if rank == 0:
+        out = {"metric": "GLUP/s", "value": value, "unit": "GLUP/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32+f64", "data": "synthetic", "config": config_dict(args.size, g),
+               "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+               "gpu_launches": int(launches_mx), "forms": forms,
+               "tensor_k_m2": K.tolist(),
+               "mixed_wk33_after_timed_blocks": [r.wk33 for r in res_mx]}
+        if k_rel is not None:
+            out["k_rel_diff_vs_fp64"] = k_rel
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_profile_case(args):
+    import poremaps_gb300 as pm
+
+    g, rots = workload(args.size)
+    with pm.Problem(rots[0], None, precision=args.profile_case, solving_algorithm=3,
+                    boundary_method=0, voxel_size=1e-5, order="jacobi") as p:
+        for _ in range(2):
+            p.block_timed(SWEEPS_PER_BLOCK, True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.profile_case:
+        return run_profile_case(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -153,6 +153,24 @@ pm_status pm_run_inp(const char* inp_path, const pm_params* overrides, pm_result
 pm_status pm_solve_tensor(const pm_params* p, const uint8_t* geom, double K[9],
                           pm_result res3[3]);
 
+/* ---- device selection, timing and re-use (bench and serving support) ---- */
+/* Select the CUDA device for problems created afterwards by this thread. */
+pm_status pm_set_device(int device);
+/* Back to the initial state (iteration 0, fields as after pm_problem_create). */
+pm_status pm_problem_reset(pm_problem* pr);
+/* n iterations, then (if check) the convergence evaluation of
+ * compute_convergence; *device_ms = CUDA-event time on the problem's stream
+ * from before the first sweep to after the reduction's read-back. */
+pm_status pm_block_timed(pm_problem* pr, int n, int check, double* permeability, double* conv,
+                         double* device_ms);
+/* Average device time of one launch of a sweep kernel of this problem's form,
+ * measured with CUDA events over n back-to-back launches on its stream
+ * (kernel 0: the form's main sweep -- the FP32 correction sweep of the mixed
+ * form, the Jacobi/red-black FP64 sweep otherwise).  The state is restored. */
+pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms);
+/* Number of kernels this library has launched in this process. */
+uint64_t pm_kernel_launches(void);
+
 /* ---- batched / serving form: many uneven samples resident at once ---- */
 typedef struct {
   size_t hbm_budget_bytes;  /* admission budget for resident problems (0 = 80% of free) */

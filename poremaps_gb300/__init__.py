@@ -79,7 +79,8 @@ EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_read_geometry", "pm_problem_create", "pm_problem_destroy", "pm_solve",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
            "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
-           "pm_run_inp", "pm_solve_tensor", "pm_server_create", "pm_server_destroy",
+           "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
+           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms"]
 
@@ -116,6 +117,12 @@ def load_library(path: str = LIB_PATH):
         "pm_write_outputs": (C.c_int, [vp]),
         "pm_run_inp": (C.c_int, [C.c_char_p, P(Params), P(Result)]),
         "pm_solve_tensor": (C.c_int, [P(Params), vp, P(C.c_double), P(Result)]),
+        "pm_set_device": (C.c_int, [C.c_int]),
+        "pm_problem_reset": (C.c_int, [vp]),
+        "pm_block_timed": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
+                                     P(C.c_double)]),
+        "pm_kernel_time": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double)]),
+        "pm_kernel_launches": (C.c_uint64, []),
         "pm_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
         "pm_server_destroy": (C.c_int, [vp]),
         "pm_server_submit": (C.c_int, [vp, P(Params), vp, P(C.c_uint64)]),
@@ -239,6 +246,31 @@ class Problem:
 
     def write_outputs(self) -> None:
         _check(load_library().pm_write_outputs(self.h))
+
+    def reset(self) -> None:
+        _check(load_library().pm_problem_reset(self.h))
+
+    def block_timed(self, n: int, check: bool = True, permeability: float = 0.0):
+        """n iterations (+ convergence check); returns (device_ms, conv, permeability)."""
+        k = C.c_double(permeability)
+        conv = C.c_double()
+        ms = C.c_double()
+        _check(load_library().pm_block_timed(self.h, n, int(check), C.byref(k), C.byref(conv),
+                                             C.byref(ms)))
+        return ms.value, conv.value, k.value
+
+    def kernel_time(self, kernel: int = 0, n: int = 20) -> float:
+        v = C.c_double()
+        _check(load_library().pm_kernel_time(self.h, kernel, n, C.byref(v)))
+        return v.value
+
+
+def set_device(device: int) -> None:
+    _check(load_library().pm_set_device(device))
+
+
+def kernel_launches() -> int:
+    return int(load_library().pm_kernel_launches())
 
 
 def run_inp(path: str, **overrides) -> Result:

@@ -183,14 +183,39 @@ pm_status iterate_n(pm_problem* pr, int n) {
   return PM_OK;
 }
 
-pm_status reduce(pm_problem* pr, int full) {
+pm_status reduce_launch(pm_problem* pr, int full) {
   int mode = (pr->precision == PM_PREC_MIXED && pr->dc_pos > 0) ? 1 : 0;
   CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
                    pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
                    pr->prm.dom_interest, pr->partials, pr->dout, pr->st));
   CK(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(double) * kRedVals, cudaMemcpyDeviceToHost,
                      pr->st));
+  return PM_OK;
+}
+
+pm_status reduce(pm_problem* pr, int full) {
+  pm_status s = reduce_launch(pr, full);
+  if (s != PM_OK) return s;
   return device_sync(pr, "reduce");
+}
+
+// Initial state: fields as set up by allocate_initial_field + reapply.
+pm_status reset_state(pm_problem* pr) {
+  CK(launch_init64(pr->F[0], pr->codes, pr->g, pr->st));
+  CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
+  if (pr->precision == PM_PREC_MIXED) {
+    CK(launch_zero32(pr->E[0], pr->g, pr->st));
+    CK(launch_zero32(pr->E[1], pr->g, pr->st));
+  }
+  pr->cur = pr->ecur = pr->dc_pos = 0;
+  pr->iteration = 0;
+  pr->perm_prev = 0.0;
+  pr->conv = 0.0;
+  pr->conv_valid = false;
+  pr->first_log = true;
+  pr->device_ms = 0.0;
+  pr->sweeps_done = 0;
+  return device_sync(pr, "reset");
 }
 
 // compute_convergence (evaluation.cc:216-262)
@@ -488,6 +513,74 @@ pm_status pm_solve(pm_problem* pr, pm_result* res) {
     return set_error(PM_ERR_NONFINITE, "non-finite permeability (conv=%g)", conv);
   return PM_OK;
 }
+
+pm_status pm_set_device(int device) {
+  CK(cudaSetDevice(device));
+  return PM_OK;
+}
+
+pm_status pm_problem_reset(pm_problem* pr) {
+  if (!pr) return set_error(PM_ERR_INVALID, "bad arguments");
+  return reset_state(pr);
+}
+
+pm_status pm_block_timed(pm_problem* pr, int n, int check, double* permeability, double* conv,
+                         double* device_ms) {
+  if (!pr || n < 0) return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s;
+  CK(cudaEventRecord(pr->ev0, pr->st));
+  if ((s = iterate_n(pr, n)) != PM_OK) return s;
+  if (check && (s = reduce_launch(pr, 0)) != PM_OK) return s;
+  CK(cudaEventRecord(pr->ev1, pr->st));
+  if ((s = device_sync(pr, "pm_block_timed")) != PM_OK) return s;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+  pr->device_ms += ms;
+  if (device_ms) *device_ms = ms;
+  if (check && permeability && conv) convergence_from(pr, pr->hout[2], permeability, conv);
+  return PM_OK;
+}
+
+pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
+  if (!pr || n <= 0 || !avg_ms) return set_error(PM_ERR_INVALID, "bad arguments");
+  if (pr->order == PM_ORDER_REFERENCE)
+    return set_error(PM_ERR_INVALID, "kernel timing is for the out-of-place forms");
+  // Repeated launches read the current state and write the scratch buffer
+  // (identical result every time), so the state is unchanged afterwards.
+  CK(cudaEventRecord(pr->ev0, pr->st));
+  for (int i = 0; i < n; ++i) {
+    if (pr->precision == PM_PREC_MIXED) {
+      if (kernel == 1) {
+        if (pr->dc_pos != 0) return set_error(PM_ERR_INVALID, "residual timing needs dc_pos 0");
+        CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list,
+                              pr->nlist, pr->g, pr->solver, pr->st));
+      } else {
+        CK(launch_dc_inner(pr->E[pr->ecur], pr->E[1 - pr->ecur], pr->R, pr->codes, pr->list,
+                           pr->nlist, pr->g, pr->solver, pr->st));
+      }
+    } else {
+      Fields<double> A = pr->F[pr->cur], B = pr->F[1 - pr->cur];
+      if (pr->order == PM_ORDER_JACOBI) {
+        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
+                          pr->st));
+      } else {
+        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 1,
+                          pr->st));
+        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 2,
+                          pr->st));
+      }
+    }
+  }
+  CK(cudaEventRecord(pr->ev1, pr->st));
+  pm_status s;
+  if ((s = device_sync(pr, "pm_kernel_time")) != PM_OK) return s;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+  *avg_ms = ms / n;
+  return PM_OK;
+}
+
+uint64_t pm_kernel_launches(void) { return (uint64_t)launches_total(); }
 
 pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double* p) {
   if (!pr) return set_error(PM_ERR_INVALID, "bad arguments");

@@ -50,6 +50,7 @@ static cudaError_t sweep_fast_s(Fields<double> A, Fields<double> B, const uint8_
   if (phase == 0) k_sweep64_fast<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
   else if (phase == 1) k_sweep64_fast<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
   else k_sweep64_fast<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -81,6 +82,7 @@ __global__ void k_dc_correct(Fields<double> x, Fields<float> e, Grid g) {
 cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
                               cudaStream_t st) {
   k_dc_correct<<<1184, 256, 0, st>>>(x, e, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -124,6 +126,7 @@ cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> 
   if (solver == 1) k_dc_residual<1><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
   else if (solver == 2) k_dc_residual<2><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
   else k_dc_residual<3><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -161,6 +164,7 @@ cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
   if (solver == 1) k_dc_inner<1><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
   else if (solver == 2) k_dc_inner<2><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
   else k_dc_inner<3><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 

@@ -58,6 +58,10 @@ struct Counts {
   long long pend_fluid;  // fluid voxels on the dom_interest zmax plane
 };
 
+// Kernel launch counter (all launch wrappers add the kernels they start).
+void count_launches(int n);
+unsigned long long launches_total();
+
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return the launch error.
 cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st);

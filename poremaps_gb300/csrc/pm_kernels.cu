@@ -4,12 +4,18 @@
 // (which is built for x86-64 without FMA contraction).
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "pm_internal.h"
 #include "pm_stencil.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace pm {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+unsigned long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 
 Grid make_grid(int nx, int ny, int nz, int bm) {
   Grid g;
@@ -89,6 +95,7 @@ __global__ void k_codes(const uint8_t* raw, uint8_t* codes, Grid g) {
 
 cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st) {
   k_codes<<<1184, 256, 0, st>>>(raw, codes, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -168,6 +175,7 @@ cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, in
   k_row_counts<<<nrows, 128, 0, st>>>(codes, g, tmp);
   k_scan_rows<<<1, 1024, 0, st>>>(tmp, nrows, tmp + nrows, count);
   k_row_fill<<<nrows, 32, 0, st>>>(codes, g, tmp + nrows, list);
+  count_launches(3);
   e = cudaGetLastError();
   cudaFreeAsync(tmp, st);
   return e;
@@ -202,6 +210,7 @@ cudaError_t launch_counts(const uint8_t* codes, const Grid& g, const int di[6],
   cudaError_t e = cudaMemsetAsync(out4, 0, 4 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   k_counts<<<592, 256, 0, st>>>(codes, g, di[0], di[1], di[2], di[3], di[4], di[5], out4);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -260,6 +269,7 @@ __global__ void k_init64(Fields<double> f, const uint8_t* codes, Grid g) {
 cudaError_t launch_init64(Fields<double> f, const uint8_t* codes, const Grid& g,
                           cudaStream_t st) {
   k_init64<<<1184, 256, 0, st>>>(f, codes, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -327,6 +337,7 @@ __global__ void k_halo64(Fields<double> f, Grid g) {
 
 cudaError_t launch_halo64(Fields<double> f, const Grid& g, cudaStream_t st) {
   k_halo64<<<592, 256, 0, st>>>(f, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -349,6 +360,7 @@ __global__ void k_reapply64(double* p, const uint8_t* codes, Grid g) {
 
 cudaError_t launch_reapply64(double* p, const uint8_t* codes, const Grid& g, cudaStream_t st) {
   k_reapply64<<<148, 256, 0, st>>>(p, codes, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -415,6 +427,7 @@ cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid&
   Grid gg = g;
   int n = n_iter;
   void* args[] = {&ff, &cc, &gg, &n};
+  count_launches(1);
   return cudaLaunchCooperativeKernel(fn, dim3(*coop_blocks), dim3(256), args, 0, st);
 }
 
@@ -450,6 +463,7 @@ static cudaError_t sweep_exact_s(Fields<double> A, Fields<double> B, const uint8
   if (phase == 0) k_sweep64_exact<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
   else if (phase == 1) k_sweep64_exact<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
   else k_sweep64_exact<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -545,6 +559,7 @@ cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full,
     k_reduce<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
                                                      di[2], di[3], di[4], di[5], partials);
   k_reduce_final<<<1, 1024, 0, st>>>(partials, out);
+  count_launches(2);
   return cudaGetLastError();
 }
 
@@ -572,6 +587,7 @@ __global__ void k_pack64(const double* f, const float* e, const uint8_t* codes, 
 cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
                           const Grid& g, double* out, cudaStream_t st) {
   k_pack64<<<1184, 256, 0, st>>>(f, e, codes, implied3, g, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -595,6 +611,7 @@ __global__ void k_pack_codes(const uint8_t* codes, Grid g, int* out) {
 
 cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st) {
   k_pack_codes<<<1184, 256, 0, st>>>(codes, g, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
