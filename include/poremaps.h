@@ -171,6 +171,29 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms);
 /* Number of kernels this library has launched in this process. */
 uint64_t pm_kernel_launches(void);
 
+/* ---- allocation-free sums (no counterpart in the reference) ----
+ * For callers that cannot let a library allocate device memory: a serving
+ * process whose HBM is reserved up front by its own admission control, or a
+ * host framework that owns every device allocation (a cudaMalloc/cudaFree
+ * inside its stream work would also synchronise the device).  Computes, over
+ * device buffers the caller owns, the nine sums behind compute_permeability /
+ * compute_convergence, over fluid voxels (geom == 0) only:
+ *   sums[0..3] = sum u, sum v, sum w, max(0, max w)
+ *   sums[4..8] = dom_interest box: sum u, sum v, sum w, sum p on its zmin plane,
+ *                sum p on its zmax plane (zeros when dom_interest is all 0 / NULL)
+ * geom, u, v, w, p: device arrays of nx*ny*nz elements, x fastest; sums: 9
+ * doubles in device memory.  Launches on `stream` (a cudaStream_t; NULL = the
+ * default stream) and returns without synchronising.  No cudaMalloc, cudaFree
+ * or allocating library call: the only scratch is a fixed device array of the
+ * library (ny*nz <= 16384 rows, 1.18 MB, held by every GPU that loads the
+ * library until exit); larger sizes return PM_ERR_INVALID.  All calls share that
+ * array, so calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address with that device current; make it before any
+ * stream capture. */
+pm_status pm_reduce_fields_noalloc(const int size[3], const uint8_t* geom, const double* u,
+                                   const double* v, const double* w, const double* p,
+                                   const int dom_interest[6], double* sums, void* stream);
+
 /* ---- batched / serving form: many uneven samples resident at once ---- */
 typedef struct {
   size_t hbm_budget_bytes;  /* admission budget for resident problems (0 = 80% of free) */

@@ -80,7 +80,8 @@ EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
            "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
            "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
-           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_server_create", "pm_server_destroy",
+           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_reduce_fields_noalloc",
+           "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms"]
 
@@ -123,6 +124,8 @@ def load_library(path: str = LIB_PATH):
                                      P(C.c_double)]),
         "pm_kernel_time": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double)]),
         "pm_kernel_launches": (C.c_uint64, []),
+        "pm_reduce_fields_noalloc": (C.c_int, [P(C.c_int), vp, vp, vp, vp, vp, P(C.c_int), vp,
+                                               vp]),
         "pm_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
         "pm_server_destroy": (C.c_int, [vp]),
         "pm_server_submit": (C.c_int, [vp, P(Params), vp, P(C.c_uint64)]),
