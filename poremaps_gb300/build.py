@@ -33,6 +33,7 @@ UNITS = [
     ("pm_api.cpp", []),
     ("pm_io.cpp", []),
     ("pm_server.cpp", []),
+    ("pm_batch.cu", []),
     ("pm_noalloc.cu", []),
 ]
 

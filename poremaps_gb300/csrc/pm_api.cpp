@@ -54,46 +54,6 @@ pm_status cuda_error(cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return cuda_error(_e, #expr); \
   } while (0)
 
-// ------------------------------------------------------------------ problem
-struct pm_problem {
-  pm_params prm;
-  Grid g;
-  cudaStream_t st = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int order = PM_ORDER_JACOBI;
-  int precision = PM_PREC_FP64;
-  int solver = 2;
-  int exact = 1;
-  // device memory
-  uint8_t* codes_base = nullptr;
-  uint8_t* codes = nullptr;
-  int* list = nullptr;
-  int nlist = 0;
-  double* f64_base[2] = {nullptr, nullptr};
-  Fields<double> F[2];
-  float* f32_base = nullptr;  // e0, e1, r
-  Fields<float> E[2], R;
-  double* partials = nullptr;
-  double* dout = nullptr;
-  double* hout = nullptr;  // pinned
-  void* scratch = nullptr;  // export buffer
-  size_t scratch_bytes = 0;
-  int coop_blocks = 0;
-  // state
-  int cur = 0;        // FP64 state buffer holding the current iterate
-  int ecur = 0;       // FP32 correction buffer holding e
-  int dc_pos = 0;     // sweeps since the last FP64 correction (mixed form)
-  int mixed_inner = 100;
-  int iteration = 0;  // next iteration index of calc_flow
-  double perm_prev = 0.0;
-  double conv = 0.0;
-  bool conv_valid = false;
-  bool first_log = true;
-  Counts counts{};
-  double phi = 0.0;
-  double device_ms = 0.0;
-  long long sweeps_done = 0;
-};
 
 namespace {
 
@@ -153,6 +113,12 @@ pm_status dc_flush(pm_problem* pr) {
   return PM_OK;
 }
 
+}  // namespace
+
+pm_status pm::problem_flush(pm_problem* pr) { return dc_flush(pr); }
+
+namespace {
+
 pm_status iterate_mixed(pm_problem* pr) {
   if (pr->dc_pos == 0) {
     CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list, pr->nlist,
@@ -163,11 +129,16 @@ pm_status iterate_mixed(pm_problem* pr) {
     pr->ecur = 1 - pr->ecur;
   }
   pr->dc_pos++;
-  if (pr->dc_pos >= pr->mixed_inner) return dc_flush(pr);
+  // the FP64 correction lands after every sweep whose iteration index is a
+  // multiple of mixed_inner (with mixed_inner = it_eval: on every iteration
+  // the reference evaluates convergence at)
+  if (pr->iteration % pr->mixed_inner == 0) return dc_flush(pr);
   return PM_OK;
 }
 
-pm_status iterate_n(pm_problem* pr, int n) {
+}  // namespace
+
+pm_status pm::iterate_n(pm_problem* pr, int n) {
   if (n <= 0) return PM_OK;
   if (pr->order == PM_ORDER_REFERENCE) {
     CK(launch_wavefront(pr->F[pr->cur], pr->codes, pr->g, pr->solver, n, &pr->coop_blocks,
@@ -176,12 +147,17 @@ pm_status iterate_n(pm_problem* pr, int n) {
     for (int i = 0; i < n; ++i) {
       pm_status s = pr->precision == PM_PREC_MIXED ? iterate_mixed(pr) : iterate64(pr);
       if (s != PM_OK) return s;
+      pr->iteration++;
+      pr->sweeps_done++;
     }
+    return PM_OK;
   }
   pr->iteration += n;
   pr->sweeps_done += n;
   return PM_OK;
 }
+
+namespace {
 
 pm_status reduce_launch(pm_problem* pr, int full) {
   int mode = (pr->precision == PM_PREC_MIXED && pr->dc_pos > 0) ? 1 : 0;
@@ -193,11 +169,15 @@ pm_status reduce_launch(pm_problem* pr, int full) {
   return PM_OK;
 }
 
-pm_status reduce(pm_problem* pr, int full) {
+}  // namespace
+
+pm_status pm::reduce(pm_problem* pr, int full) {
   pm_status s = reduce_launch(pr, full);
   if (s != PM_OK) return s;
   return device_sync(pr, "reduce");
 }
+
+namespace {
 
 // Initial state: fields as set up by allocate_initial_field + reapply.
 pm_status reset_state(pm_problem* pr) {
@@ -218,8 +198,10 @@ pm_status reset_state(pm_problem* pr) {
   return device_sync(pr, "reset");
 }
 
+}  // namespace
+
 // compute_convergence (evaluation.cc:216-262)
-void convergence_from(pm_problem* pr, double velz_sum, double* perm, double* conv) {
+void pm::convergence_from(pm_problem* pr, double velz_sum, double* perm, double* conv) {
   int flcount = (int)(double)pr->counts.fluid;
   double sum = flcount == 0 ? 0.0 : velz_sum;
   double mean = sum / flcount;
@@ -227,6 +209,8 @@ void convergence_from(pm_problem* pr, double velz_sum, double* perm, double* con
   *conv = fabs(cur - *perm) / cur;
   *perm = cur;
 }
+
+namespace {
 
 // compute_permeability (evaluation.cc:54-211) from the device sums
 void permeability_from(pm_problem* pr, const double* s, pm_result* r) {

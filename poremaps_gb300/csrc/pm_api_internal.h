@@ -4,6 +4,48 @@
 #include <cuda_runtime.h>
 
 #include "../../include/poremaps.h"
+#include "pm_internal.h"
+
+// One device-resident domain (the state behind a pm_problem handle).
+struct pm_problem {
+  pm_params prm;
+  pm::Grid g;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int order = PM_ORDER_JACOBI;
+  int precision = PM_PREC_FP64;
+  int solver = 2;
+  int exact = 1;
+  // device memory
+  uint8_t* codes_base = nullptr;
+  uint8_t* codes = nullptr;
+  int* list = nullptr;
+  int nlist = 0;
+  double* f64_base[2] = {nullptr, nullptr};
+  pm::Fields<double> F[2];
+  float* f32_base = nullptr;  // e0, e1, r
+  pm::Fields<float> E[2], R;
+  double* partials = nullptr;
+  double* dout = nullptr;
+  double* hout = nullptr;  // pinned
+  void* scratch = nullptr;  // export buffer
+  size_t scratch_bytes = 0;
+  int coop_blocks = 0;
+  // state
+  int cur = 0;        // FP64 state buffer holding the current iterate
+  int ecur = 0;       // FP32 correction buffer holding e
+  int dc_pos = 0;     // sweeps since the last FP64 correction (mixed form)
+  int mixed_inner = 100;
+  int iteration = 0;  // next iteration index of calc_flow
+  double perm_prev = 0.0;
+  double conv = 0.0;
+  bool conv_valid = false;
+  bool first_log = true;
+  pm::Counts counts{};
+  double phi = 0.0;
+  double device_ms = 0.0;
+  long long sweeps_done = 0;
+};
 
 namespace pm {
 
@@ -15,5 +57,11 @@ size_t problem_device_bytes(const pm_params* p);
 const pm_params* problem_params(const pm_problem* pr);
 long long problem_nvox(const pm_problem* pr);
 cudaStream_t problem_stream(const pm_problem* pr);
+// calc_flow pieces shared with the server
+pm_status iterate_n(pm_problem* pr, int n);
+// mixed form: fold the FP32 correction into the FP64 state (no-op otherwise)
+pm_status problem_flush(pm_problem* pr);
+pm_status reduce(pm_problem* pr, int full);
+void convergence_from(pm_problem* pr, double velz_sum, double* perm, double* conv);
 
 }  // namespace pm

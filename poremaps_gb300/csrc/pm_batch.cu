@@ -1,0 +1,117 @@
+// Batched sweeps: one launch advances every resident sample by one sweep.
+//
+// The work is a table of items (sample, first fluid voxel, count) built from
+// the samples' fluid lists; thread blocks walk the table with a grid stride,
+// so samples of very different sizes share one launch and the device stays
+// full while small samples finish and new ones arrive.  Each voxel runs the
+// same device function as the single-problem kernels (pm_stencil.cuh), so a
+// sample's fields are identical whether it is solved alone or in a batch.
+#include "pm_batch.h"
+#include "pm_stencil.cuh"
+
+namespace pm {
+
+namespace {
+
+__device__ __forceinline__ const SampleDesc& desc_of(const SampleDesc* d, int s) { return d[s]; }
+
+template <typename F>
+__device__ __forceinline__ void walk_items(const WorkItem* items, int nitems, F f) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    for (int q = threadIdx.x; q < w.count; q += blockDim.x) f(w.sample, w.start + q);
+  }
+}
+
+__global__ void k_batch_residual(const SampleDesc* d, const WorkItem* items, int nitems) {
+  walk_items(items, nitems, [&](int s, int q) {
+    const SampleDesc& sd = desc_of(d, s);
+    const Fields<float>& E = sd.ecur0 ? sd.E1 : sd.E0;
+    int lin = sd.list[q];
+    if (sd.solver == 3) dc_residual_voxel<3>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
+    else if (sd.solver == 2) dc_residual_voxel<2>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
+    else dc_residual_voxel<1>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
+  });
+}
+
+__global__ void k_batch_inner(const SampleDesc* d, const WorkItem* items, int nitems, int round) {
+  walk_items(items, nitems, [&](int s, int q) {
+    const SampleDesc& sd = desc_of(d, s);
+    const int a = (sd.ecur0 + round - 1) & 1;
+    const Fields<float>& Ein = a ? sd.E1 : sd.E0;
+    const Fields<float>& Eout = a ? sd.E0 : sd.E1;
+    int lin = sd.list[q];
+    if (sd.solver == 3) dc_inner_voxel<3>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
+    else if (sd.solver == 2) dc_inner_voxel<2>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
+    else dc_inner_voxel<1>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
+  });
+}
+
+__global__ void k_batch_correct(const SampleDesc* d, const WorkItem* items, int nitems,
+                                int rounds) {
+  walk_items(items, nitems, [&](int s, int q) {
+    const SampleDesc& sd = desc_of(d, s);
+    const int a = (sd.ecur0 + rounds - 1) & 1;
+    dc_correct_voxel(sd.X0, a ? sd.E1 : sd.E0, sd.g, sd.list[q]);
+  });
+}
+
+__global__ void k_batch_sweep64(const SampleDesc* d, const WorkItem* items, int nitems,
+                                int round) {
+  walk_items(items, nitems, [&](int s, int q) {
+    const SampleDesc& sd = desc_of(d, s);
+    const int a = (sd.xcur0 + round) & 1;
+    const Fields<double>& A = a ? sd.X1 : sd.X0;
+    const Fields<double>& B = a ? sd.X0 : sd.X1;
+    int lin = sd.list[q];
+    if (sd.solver == 3) sweep64_voxel<3, 0, false>(A, B, sd.codes, sd.g, lin);
+    else if (sd.solver == 2) sweep64_voxel<2, 0, false>(A, B, sd.codes, sd.g, lin);
+    else sweep64_voxel<1, 0, false>(A, B, sd.codes, sd.g, lin);
+  });
+}
+
+// Per item: sum of w over its fluid voxels (fixed order: strided per thread,
+// then a fixed tree), from the FP64 state selected by `round` parity.
+__global__ void k_batch_sumw(const SampleDesc* d, const WorkItem* items, int nitems, int round,
+                             double* out) {
+  __shared__ double sh[1024];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const WorkItem w = items[it];
+    const SampleDesc& sd = desc_of(d, w.sample);
+    const Fields<double>& X = ((sd.xcur0 + round) & 1) ? sd.X1 : sd.X0;
+    double acc = 0.0;
+    for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
+      int x, y, z;
+      lin_to_xyz(sd.list[w.start + q], sd.g, x, y, z);
+      acc += X.w[(long long)z * sd.g.pl64 + (long long)y * sd.g.px64 + x];
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < (unsigned)o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[it] = sh[0];
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, int nitems,
+                         int round, int threads, int blocks, double* out, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  int grid = blocks > 0 ? (blocks < nitems ? blocks : nitems) : nitems;
+  switch (kind) {
+    case kBatchResidual: k_batch_residual<<<grid, threads, 0, st>>>(d, items, nitems); break;
+    case kBatchInner: k_batch_inner<<<grid, threads, 0, st>>>(d, items, nitems, round); break;
+    case kBatchCorrect: k_batch_correct<<<grid, threads, 0, st>>>(d, items, nitems, round); break;
+    case kBatchSweep64: k_batch_sweep64<<<grid, threads, 0, st>>>(d, items, nitems, round); break;
+    case kBatchSumW: k_batch_sumw<<<grid, threads, 0, st>>>(d, items, nitems, round, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace pm

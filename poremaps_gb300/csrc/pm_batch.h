@@ -1,0 +1,35 @@
+// Batched (many-sample) sweep kernels: descriptors and launcher.
+#pragma once
+
+#include "pm_internal.h"
+
+namespace pm {
+
+// One resident sample as the batched kernels see it.
+struct SampleDesc {
+  Grid g;
+  Fields<double> X0, X1;  // FP64 state (mixed form: X0 is x; FP64 form: ping-pong)
+  Fields<float> E0, E1, R;
+  const uint8_t* codes;
+  const int* list;
+  int solver;
+  int ecur0;  // correction buffer the residual writes (mixed form)
+  int xcur0;  // FP64 buffer holding the state at the start of a block (FP64 form)
+};
+
+// A contiguous run of one sample's fluid list.
+struct WorkItem {
+  int sample;
+  int start;
+  int count;
+};
+
+enum { kBatchResidual = 0, kBatchInner = 1, kBatchCorrect = 2, kBatchSweep64 = 3, kBatchSumW = 4 };
+
+// kind: kBatch*; round: sweep index inside the block (inner / sweep64), the
+// number of rounds (correct), or the state parity (sumw).  blocks <= 0: one
+// block per item.
+cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, int nitems,
+                         int round, int threads, int blocks, double* out, cudaStream_t st);
+
+}  // namespace pm

@@ -19,22 +19,8 @@ template <int SOLVER, int PHASE>
 __global__ void __launch_bounds__(256) k_sweep64_fast(Fields<double> A, Fields<double> B,
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
-  const long long px = g.px64, pl = g.pl64;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
-    int lin = list[q];
-    int xp = lin % g.nx;
-    int r = lin / g.nx;
-    int yp = r % g.ny, zp = r / g.ny;
-    if (PHASE && (((xp + yp + zp) & 1) != PHASE - 1)) continue;
-    int x = xp + 2, y = yp + 2, z = zp + 2;
-    int code = codes[((long long)z * g.NY + y) * g.pxc + x];
-    long long c = (long long)z * pl + (long long)y * px + x;
-    Stencil<double> s;
-    gather<double, PHASE>(s, A, B, c, x, y, z, g, px, pl);
-    double un, vn, wn, pn;
-    update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
-    write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, list[q]);
 }
 
 cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* codes,
@@ -86,36 +72,13 @@ cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
   return cudaGetLastError();
 }
 
-// r = F(x) - x in FP64 (stored FP32) and the first correction e1 = r.  On the
-// last interior plane the state stores the swept pressure (the reapplied 3 is
-// implied), so its residual is taken against that stored value.
+// r = F(x) - x in FP64 (stored FP32) and the first correction e1 = r.
 template <int SOLVER>
 __global__ void __launch_bounds__(256) k_dc_residual(Fields<double> X, Fields<float> R,
                                                      Fields<float> E, const uint8_t* codes,
                                                      const int* list, int nlist, Grid g) {
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
-    int lin = list[q];
-    int xp = lin % g.nx;
-    int rr = lin / g.nx;
-    int yp = rr % g.ny, zp = rr / g.ny;
-    int x = xp + 2, y = yp + 2, z = zp + 2;
-    int code = codes[((long long)z * g.NY + y) * g.pxc + x];
-    long long c = (long long)z * g.pl64 + (long long)y * g.px64 + x;
-    Stencil<double> s;
-    gather<double, 0>(s, X, X, c, x, y, z, g, g.px64, g.pl64);
-    double un, vn, wn, pn;
-    update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
-    // the stored pressure (swept, pre-reapply on the last interior plane)
-    const double pstored = (z == g.NZ - 3) ? __ldg(X.p + c) : s.pc;
-    float ru = (float)(un - s.uc), rv = (float)(vn - s.vc), rw = (float)(wn - s.wc),
-          rp = (float)(pn - pstored);
-    long long c32 = (long long)z * g.pl32 + (long long)y * g.px32 + x;
-    R.u[c32] = ru;
-    R.v[c32] = rv;
-    R.w[c32] = rw;
-    R.p[c32] = rp;
-    write_voxel<float, true>(E, c32, x, y, z, g, g.px32, g.pl32, ru, rv, rw, rp);
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    dc_residual_voxel<SOLVER>(X, R, E, codes, g, list[q]);
 }
 
 cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> e,
@@ -135,25 +98,8 @@ template <int SOLVER>
 __global__ void __launch_bounds__(256) k_dc_inner(Fields<float> E, Fields<float> E2,
                                                   Fields<float> R, const uint8_t* codes,
                                                   const int* list, int nlist, Grid g) {
-  const long long px = g.px32, pl = g.pl32;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
-    int lin = list[q];
-    int xp = lin % g.nx;
-    int rr = lin / g.nx;
-    int yp = rr % g.ny, zp = rr / g.ny;
-    int x = xp + 2, y = yp + 2, z = zp + 2;
-    int code = codes[((long long)z * g.NY + y) * g.pxc + x];
-    long long c = (long long)z * pl + (long long)y * px + x;
-    Stencil<float> s;
-    gather<float, 0, true, 2>(s, E, E, c, x, y, z, g, px, pl);
-    float un, vn, wn, pn;
-    update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
-    un += __ldg(R.u + c);
-    vn += __ldg(R.v + c);
-    wn += __ldg(R.w + c);
-    pn += __ldg(R.p + c);
-    write_voxel<float, true>(E2, c, x, y, z, g, px, pl, un, vn, wn, pn);
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
 }
 
 cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,

@@ -436,22 +436,8 @@ template <int SOLVER, int PHASE>
 __global__ void __launch_bounds__(256) k_sweep64_exact(Fields<double> A, Fields<double> B,
                                                        const uint8_t* codes, const int* list,
                                                        int nlist, Grid g) {
-  const long long px = g.px64, pl = g.pl64;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
-    int lin = list[q];
-    int xp = lin % g.nx;
-    int r = lin / g.nx;
-    int yp = r % g.ny, zp = r / g.ny;
-    if (PHASE && (((xp + yp + zp) & 1) != PHASE - 1)) continue;
-    int x = xp + 2, y = yp + 2, z = zp + 2;
-    int code = codes[((long long)z * g.NY + y) * g.pxc + x];
-    long long c = (long long)z * pl + (long long)y * px + x;
-    Stencil<double> s;
-    gather<double, PHASE>(s, A, B, c, x, y, z, g, px, pl);
-    double un, vn, wn, pn;
-    update_exact<SOLVER>(s, code, un, vn, wn, pn);
-    write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    sweep64_voxel<SOLVER, PHASE, true>(A, B, codes, g, list[q]);
 }
 
 template <int SOLVER>

@@ -1,0 +1,496 @@
+// Batched / continuously batching solver (pm_server_* of include/poremaps.h).
+//
+// Requests queue on the host.  A scheduling round (pm_server_step):
+//   1. admits queued requests first come first served while their device
+//      footprint fits the HBM budget and a slot is free (set-up on the
+//      device, then one sweep so every resident sample sits at the start of
+//      an it_eval block: the reference evaluates convergence after the sweeps
+//      it_eval, 2 it_eval, ...);
+//   2. runs one it_eval block for all resident samples: it_eval batched
+//      launches walking a work table of (sample, fluid-voxel run) items,
+//      captured once per change of the resident set in a CUDA graph, then a
+//      per-item sum of w;
+//   3. evaluates compute_convergence per sample (the reference's stop rule)
+//      and retires the finished ones (permeability, completion record,
+//      device memory freed) without touching the others.
+// A sample's values do not depend on what else is resident: every voxel runs
+// the same device code as the single-problem path, and its sums follow its own
+// items in a fixed order.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <mutex>
+#include <vector>
+
+#include "../../include/poremaps.h"
+#include "pm_api_internal.h"
+#include "pm_batch.h"
+
+using namespace pm;
+
+namespace {
+
+struct Req {
+  uint64_t ticket;
+  pm_params prm;
+  std::vector<uint8_t> geom;
+  double submit_ms;
+};
+
+struct Res {
+  uint64_t ticket;
+  pm_problem* pr;
+  double submit_ms, admit_ms;
+  size_t bytes;
+  double perm = 0.0, conv = 0.0;
+  bool conv_valid = false;
+  int last_check = 0;
+  int it = 0;  // next iteration index
+  int item0 = 0, nitems = 0;
+};
+
+}  // namespace
+
+struct pm_server {
+  pm_server_config cfg;
+  std::mutex mu;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::deque<Req> queue;
+  std::vector<Res> res;
+  std::deque<pm_completion> done;
+  size_t budget = 0, used = 0;
+  uint64_t next_ticket = 1;
+  std::chrono::steady_clock::time_point t0;
+  int block = 0;  // sweeps per scheduling round = it_eval of the requests
+  std::vector<SampleDesc> h_desc;
+  std::vector<WorkItem> h_items;
+  SampleDesc* d_desc = nullptr;
+  size_t cap_desc = 0;
+  WorkItem* d_items = nullptr;
+  size_t cap_items = 0;
+  double* d_part = nullptr;
+  double* h_part = nullptr;
+  size_t cap_part = 0;
+  bool dirty = true;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_kernels = 0;
+  int threads = 256, chunk = 8192;
+  long long tuned_for = -1;
+  double busy_ms = 0.0;
+  unsigned long long lups = 0;
+};
+
+namespace {
+
+double now_ms(pm_server* s) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - s->t0)
+      .count();
+}
+
+#define SCK(expr)                                        \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return cuda_error(_e, #expr); \
+  } while (0)
+
+template <typename T>
+pm_status grow(T** d, size_t* cap, size_t n) {
+  if (n <= *cap) return PM_OK;
+  size_t c = std::max(n, *cap * 2 + 16);
+  if (*d) cudaFree(*d);
+  *d = nullptr;
+  SCK(cudaMalloc((void**)d, c * sizeof(T)));
+  *cap = c;
+  return PM_OK;
+}
+
+void complete(pm_server* s, uint64_t ticket, pm_status st, const pm_result* r, double submit,
+              double admit) {
+  pm_completion c;
+  memset(&c, 0, sizeof c);
+  c.ticket = ticket;
+  c.status = st;
+  if (r) c.result = *r;
+  c.submit_ms = submit;
+  c.admit_ms = admit;
+  c.finish_ms = now_ms(s);
+  s->done.push_back(c);
+}
+
+void drop_graph(pm_server* s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  s->gexec = nullptr;
+}
+
+pm_status admit(pm_server* s) {
+  while (!s->queue.empty() && (int)s->res.size() < s->cfg.max_resident) {
+    Req& q = s->queue.front();
+    pm_params p = q.prm;
+    p.precision = s->cfg.precision;
+    p.order = PM_ORDER_JACOBI;
+    p.write_log = 0;
+    p.mixed_inner = p.it_eval;  // corrections after iterations 0, it_eval, 2 it_eval, ...
+    size_t bytes = problem_device_bytes(&p);
+    if (s->used + bytes > s->budget) {
+      if (s->res.empty()) {  // can never fit: fail it instead of blocking the queue
+        pm_status e = set_error(PM_ERR_NOMEM, "request needs %zu bytes, budget %zu", bytes,
+                                s->budget);
+        complete(s, q.ticket, e, nullptr, q.submit_ms, now_ms(s));
+        s->queue.pop_front();
+        continue;
+      }
+      break;
+    }
+    pm_problem* pr = nullptr;
+    pm_status st = pm_problem_create(&p, q.geom.data(), &pr);
+    if (st != PM_OK) {
+      complete(s, q.ticket, st, nullptr, q.submit_ms, now_ms(s));
+      s->queue.pop_front();
+      continue;
+    }
+    // iteration 0 on its own: afterwards every block ends on a check iteration
+    if ((st = iterate_n(pr, 1)) == PM_OK) st = problem_flush(pr);
+    if (st == PM_OK && cudaStreamSynchronize(problem_stream(pr)) != cudaSuccess)
+      st = cuda_error(cudaGetLastError(), "admission sweep");
+    if (st != PM_OK) {
+      pm_problem_destroy(pr);
+      complete(s, q.ticket, st, nullptr, q.submit_ms, now_ms(s));
+      s->queue.pop_front();
+      continue;
+    }
+    Res r;
+    r.ticket = q.ticket;
+    r.pr = pr;
+    r.submit_ms = q.submit_ms;
+    r.admit_ms = now_ms(s);
+    r.bytes = bytes;
+    r.it = 1;
+    s->res.push_back(r);
+    s->used += bytes;
+    s->queue.pop_front();
+    s->dirty = true;
+  }
+  return PM_OK;
+}
+
+void build_items(pm_server* s, int chunk) {
+  s->h_items.clear();
+  for (size_t i = 0; i < s->res.size(); ++i) {
+    Res& r = s->res[i];
+    r.item0 = (int)s->h_items.size();
+    int n = r.pr->nlist;
+    for (int a = 0; a < n; a += chunk) s->h_items.push_back({(int)i, a, std::min(chunk, n - a)});
+    r.nitems = (int)s->h_items.size() - r.item0;
+  }
+}
+
+pm_status upload(pm_server* s) {
+  pm_status e;
+  if ((e = grow(&s->d_desc, &s->cap_desc, s->h_desc.size())) != PM_OK) return e;
+  if ((e = grow(&s->d_items, &s->cap_items, s->h_items.size())) != PM_OK) return e;
+  if (s->h_items.size() > s->cap_part) {
+    if (s->d_part) cudaFree(s->d_part);
+    if (s->h_part) cudaFreeHost(s->h_part);
+    s->d_part = nullptr;
+    s->h_part = nullptr;
+    size_t c = s->h_items.size() * 2 + 16;
+    SCK(cudaMalloc((void**)&s->d_part, c * sizeof(double)));
+    SCK(cudaMallocHost((void**)&s->h_part, c * sizeof(double)));
+    s->cap_part = c;
+  }
+  SCK(cudaMemcpyAsync(s->d_desc, s->h_desc.data(), s->h_desc.size() * sizeof(SampleDesc),
+                      cudaMemcpyHostToDevice, s->st));
+  SCK(cudaMemcpyAsync(s->d_items, s->h_items.data(), s->h_items.size() * sizeof(WorkItem),
+                      cudaMemcpyHostToDevice, s->st));
+  SCK(cudaStreamSynchronize(s->st));
+  return PM_OK;
+}
+
+bool mixed(const pm_server* s) { return s->cfg.precision == PM_PREC_MIXED; }
+
+// The launches of one block (recorded into a graph or issued directly).
+pm_status issue_block(pm_server* s, int* nk) {
+  const int n = (int)s->h_items.size(), T = s->threads;
+  int k = 0;
+  if (mixed(s)) {
+    SCK(launch_batch(kBatchResidual, s->d_desc, s->d_items, n, 0, T, 0, nullptr, s->st));
+    ++k;
+    for (int r = 1; r < s->block; ++r, ++k)
+      SCK(launch_batch(kBatchInner, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st));
+    SCK(launch_batch(kBatchCorrect, s->d_desc, s->d_items, n, s->block, T, 0, nullptr, s->st));
+    SCK(launch_batch(kBatchSumW, s->d_desc, s->d_items, n, 0, T, 0, s->d_part, s->st));
+    k += 2;
+  } else {
+    for (int r = 0; r < s->block; ++r, ++k)
+      SCK(launch_batch(kBatchSweep64, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st));
+    SCK(launch_batch(kBatchSumW, s->d_desc, s->d_items, n, s->block, T, 0, s->d_part, s->st));
+    ++k;
+  }
+  *nk = k;
+  return PM_OK;
+}
+
+// Time the main batched sweep for a few (threads, chunk) shapes on the current
+// resident set and keep the fastest.  Safe at a block boundary: the timed
+// launches only write buffers the next block's first sweep rewrites.
+pm_status autotune(pm_server* s) {
+  static const int kThreads[] = {128, 256, 512};
+  static const int kChunks[] = {2048, 8192, 32768};
+  long long total = 0;
+  for (auto& r : s->res) total += r.pr->nlist;
+  if (s->tuned_for > 0 && total < 4 * s->tuned_for && 4 * total > s->tuned_for) return PM_OK;
+  float best = 1e30f;
+  int bt = s->threads, bc = s->chunk;
+  const int kind = mixed(s) ? kBatchInner : kBatchSweep64;
+  for (int c : kChunks) {
+    build_items(s, c);
+    pm_status e = upload(s);
+    if (e != PM_OK) return e;
+    for (int t : kThreads) {
+      SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
+                       s->st));
+      SCK(cudaEventRecord(s->e0, s->st));
+      for (int i = 0; i < 3; ++i)
+        SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
+                         s->st));
+      SCK(cudaEventRecord(s->e1, s->st));
+      SCK(cudaEventSynchronize(s->e1));
+      float ms = 0.f;
+      SCK(cudaEventElapsedTime(&ms, s->e0, s->e1));
+      if (ms < best) { best = ms; bt = t; bc = c; }
+    }
+  }
+  s->threads = bt;
+  s->chunk = bc;
+  s->tuned_for = total;
+  return PM_OK;
+}
+
+pm_status rebuild(pm_server* s) {
+  s->h_desc.clear();
+  for (auto& r : s->res) {
+    pm_problem* pr = r.pr;
+    SampleDesc d;
+    memset(&d, 0, sizeof d);
+    d.g = pr->g;
+    d.codes = pr->codes;
+    d.list = pr->list;
+    d.solver = pr->solver;
+    if (mixed(s)) {
+      d.X0 = pr->F[pr->cur];
+      d.X1 = pr->F[1 - pr->cur];
+      d.E0 = pr->E[0];
+      d.E1 = pr->E[1];
+      d.R = pr->R;
+      d.ecur0 = 0;
+      d.xcur0 = 0;
+    } else {
+      d.X0 = pr->F[0];
+      d.X1 = pr->F[1];
+      d.xcur0 = pr->cur;
+    }
+    s->h_desc.push_back(d);
+  }
+  pm_status e;
+  if (s->cfg.autotune && (e = autotune(s)) != PM_OK) return e;
+  build_items(s, s->chunk);
+  if ((e = upload(s)) != PM_OK) return e;
+  drop_graph(s);
+  s->dirty = false;
+  return PM_OK;
+}
+
+pm_status run_block(pm_server* s) {
+  pm_status e;
+  int nk = 0;
+  if (s->cfg.use_graphs && !s->gexec) {
+    cudaGraph_t g = nullptr;
+    SCK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    e = issue_block(s, &nk);
+    cudaError_t ce = cudaStreamEndCapture(s->st, &g);
+    if (e != PM_OK) {
+      if (g) cudaGraphDestroy(g);
+      return e;
+    }
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphInstantiate");
+    s->graph_kernels = nk;
+  }
+  SCK(cudaEventRecord(s->e0, s->st));
+  if (s->gexec) {
+    SCK(cudaGraphLaunch(s->gexec, s->st));
+    count_launches(s->graph_kernels);
+  } else if ((e = issue_block(s, &nk)) != PM_OK) {
+    return e;
+  }
+  SCK(cudaMemcpyAsync(s->h_part, s->d_part, s->h_items.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost, s->st));
+  SCK(cudaEventRecord(s->e1, s->st));
+  SCK(cudaStreamSynchronize(s->st));
+  float ms = 0.f;
+  SCK(cudaEventElapsedTime(&ms, s->e0, s->e1));
+  s->busy_ms += ms;
+  for (auto& r : s->res) s->lups += (unsigned long long)r.pr->g.nvox * s->block;
+  return PM_OK;
+}
+
+pm_status after_block(pm_server* s) {
+  std::vector<Res> keep;
+  bool changed = false;
+  for (auto& r : s->res) {
+    pm_problem* pr = r.pr;
+    r.it += s->block;
+    pr->iteration = r.it;
+    pr->sweeps_done = r.it;
+    pr->dc_pos = 0;
+    if (!mixed(s)) pr->cur = (pr->cur + s->block) & 1;
+    const pm_params& p = pr->prm;
+    const int last = r.it - 1;
+    if (last % p.it_eval == 0 && last > 1000) {
+      double sum = 0.0;
+      for (int k = 0; k < r.nitems; ++k) sum += s->h_part[r.item0 + k];
+      convergence_from(pr, sum, &r.perm, &r.conv);
+      r.conv_valid = true;
+      r.last_check = last;
+    }
+    bool finished = (r.conv_valid && !(r.conv >= p.eps)) || r.it >= p.max_iter;
+    if (!finished) {
+      keep.push_back(r);
+      continue;
+    }
+    pm_result out;
+    memset(&out, 0, sizeof out);
+    pm_status st = pm_compute_permeability(pr, &out);
+    out.iterations = r.last_check;
+    out.sweeps = r.it;
+    out.conv = r.conv;
+    out.converged = r.conv_valid && r.conv < p.eps;
+    out.permeability = r.perm;
+    if (st == PM_OK && (!isfinite(out.wk33) || !isfinite(r.perm))) st = PM_ERR_NONFINITE;
+    complete(s, r.ticket, st, &out, r.submit_ms, r.admit_ms);
+    pm_problem_destroy(pr);
+    s->used -= r.bytes;
+    changed = true;
+  }
+  s->res.swap(keep);
+  if (changed || (!mixed(s) && (s->block & 1))) s->dirty = true;
+  return PM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pm_status pm_server_create(const pm_server_config* cfg, pm_server** out) {
+  if (!out) return set_error(PM_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  pm_server* s = new pm_server();
+  if (cfg) s->cfg = *cfg;
+  else memset(&s->cfg, 0, sizeof s->cfg);
+  if (s->cfg.precision != PM_PREC_FP64 && s->cfg.precision != PM_PREC_MIXED) {
+    delete s;
+    return set_error(PM_ERR_INVALID, "bad precision");
+  }
+  if (s->cfg.max_resident <= 0) s->cfg.max_resident = 1024;
+  size_t fr = 0, tot = 0;
+  cudaError_t e = cudaMemGetInfo(&fr, &tot);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_error(e, "cudaMemGetInfo");
+  }
+  s->budget = s->cfg.hbm_budget_bytes ? s->cfg.hbm_budget_bytes : (size_t)(0.8 * (double)fr);
+  if ((e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&s->e0)) != cudaSuccess ||
+      (e = cudaEventCreate(&s->e1)) != cudaSuccess) {
+    pm_server_destroy(s);
+    return cuda_error(e, "server stream/events");
+  }
+  s->t0 = std::chrono::steady_clock::now();
+  *out = s;
+  return PM_OK;
+}
+
+pm_status pm_server_destroy(pm_server* s) {
+  if (!s) return PM_OK;
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (auto& r : s->res) pm_problem_destroy(r.pr);
+  drop_graph(s);
+  cudaFree(s->d_desc);
+  cudaFree(s->d_items);
+  cudaFree(s->d_part);
+  if (s->h_part) cudaFreeHost(s->h_part);
+  if (s->e0) cudaEventDestroy(s->e0);
+  if (s->e1) cudaEventDestroy(s->e1);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+  return PM_OK;
+}
+
+pm_status pm_server_submit(pm_server* s, const pm_params* p, const uint8_t* geom,
+                           uint64_t* ticket) {
+  if (!s || !p || !geom || !ticket) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (p->size[0] < 1 || p->size[1] < 1 || p->size[2] < 1 || p->it_eval <= 0)
+    return set_error(PM_ERR_INVALID, "bad request size or it_eval");
+  if (s->block == 0) s->block = p->it_eval;
+  if (p->it_eval != s->block)
+    return set_error(PM_ERR_INVALID, "server runs it_eval blocks of %d sweeps, request has %d",
+                     s->block, p->it_eval);
+  if (s->cfg.precision == PM_PREC_MIXED && p->solving_algorithm == 1)
+    return set_error(PM_ERR_INVALID, "mixed precision needs solver 2 or 3");
+  Req q;
+  q.ticket = s->next_ticket++;
+  q.prm = *p;
+  size_t n = (size_t)p->size[0] * p->size[1] * p->size[2];
+  q.geom.assign(geom, geom + n);
+  q.submit_ms = now_ms(s);
+  s->queue.push_back(std::move(q));
+  *ticket = s->queue.back().ticket;
+  return PM_OK;
+}
+
+pm_status pm_server_step(pm_server* s, int* active) {
+  if (!s) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  pm_status e;
+  if ((e = admit(s)) != PM_OK) return e;
+  if (!s->res.empty()) {
+    if (s->dirty && (e = rebuild(s)) != PM_OK) return e;
+    if ((e = run_block(s)) != PM_OK) return e;
+    if ((e = after_block(s)) != PM_OK) return e;
+    if ((e = admit(s)) != PM_OK) return e;
+  }
+  if (active) *active = (int)(s->res.size() + s->queue.size());
+  return PM_OK;
+}
+
+pm_status pm_server_poll(pm_server* s, pm_completion* out, int max, int* n) {
+  if (!s || !n || (max > 0 && !out)) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  int k = 0;
+  while (k < max && !s->done.empty()) {
+    out[k++] = s->done.front();
+    s->done.pop_front();
+  }
+  *n = k;
+  return PM_OK;
+}
+
+pm_status pm_server_stats(pm_server* s, double* busy_ms, double* wall_ms, uint64_t* lups) {
+  if (!s) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (busy_ms) *busy_ms = s->busy_ms;
+  if (wall_ms) *wall_ms = now_ms(s);
+  if (lups) *lups = s->lups;
+  return PM_OK;
+}
+
+double pm_server_clock_ms(pm_server* s) { return s ? now_ms(s) : 0.0; }
+
+}  // extern "C"

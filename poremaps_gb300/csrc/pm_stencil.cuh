@@ -253,4 +253,112 @@ __device__ __forceinline__ void write_voxel(const Fields<T>& B, long long c, int
   }
 }
 
+
+// ------------------------------------------------------------------ per-voxel bodies
+// Shared by the single-problem kernels and the batched (many-sample) kernels,
+// so a sample computes exactly the same values alone and in a batch.
+
+// Interior linear index (x fastest) -> padded coordinates.
+__device__ __forceinline__ void lin_to_xyz(int lin, const Grid& g, int& x, int& y, int& z) {
+  int xp = lin % g.nx;
+  int r = lin / g.nx;
+  x = xp + 2;
+  y = r % g.ny + 2;
+  z = r / g.ny + 2;
+}
+
+// One voxel of an FP64 sweep (Jacobi phase 0, red 1, black 2) from A into B.
+template <int SOLVER, int PHASE, bool EXACT>
+__device__ __forceinline__ void sweep64_voxel(const Fields<double>& A, const Fields<double>& B,
+                                              const uint8_t* codes, const Grid& g, int lin) {
+  int x, y, z;
+  lin_to_xyz(lin, g, x, y, z);
+  if (PHASE && (((x + y + z) & 1) != PHASE - 1)) return;  // (x+y+z) - 6 has the same parity
+  const long long px = g.px64, pl = g.pl64;
+  int code = codes[((long long)z * g.NY + y) * g.pxc + x];
+  long long c = (long long)z * pl + (long long)y * px + x;
+  Stencil<double> s;
+  gather<double, PHASE>(s, A, B, c, x, y, z, g, px, pl);
+  double un, vn, wn, pn;
+  if (EXACT) update_exact<SOLVER>(s, code, un, vn, wn, pn);
+  else update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
+  write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
+}
+
+// r = F(x) - x (FP64, stored FP32) and the first correction e1 = r.  On the
+// last interior plane the state stores the swept pressure (the reapplied 3 is
+// implied), so its residual is taken against that stored value.
+template <int SOLVER>
+__device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, const Fields<float>& R,
+                                                  const Fields<float>& E, const uint8_t* codes,
+                                                  const Grid& g, int lin) {
+  int x, y, z;
+  lin_to_xyz(lin, g, x, y, z);
+  int code = codes[((long long)z * g.NY + y) * g.pxc + x];
+  long long c = (long long)z * g.pl64 + (long long)y * g.px64 + x;
+  Stencil<double> s;
+  gather<double, 0>(s, X, X, c, x, y, z, g, g.px64, g.pl64);
+  double un, vn, wn, pn;
+  update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
+  const double pstored = (z == g.NZ - 3) ? __ldg(X.p + c) : s.pc;
+  float ru = (float)(un - s.uc), rv = (float)(vn - s.vc), rw = (float)(wn - s.wc),
+        rp = (float)(pn - pstored);
+  long long c32 = (long long)z * g.pl32 + (long long)y * g.px32 + x;
+  R.u[c32] = ru;
+  R.v[c32] = rv;
+  R.w[c32] = rw;
+  R.p[c32] = rp;
+  write_voxel<float, true>(E, c32, x, y, z, g, g.px32, g.pl32, ru, rv, rw, rp);
+}
+
+// e2 = L(e) + r (FP32 correction sweep).
+template <int SOLVER>
+__device__ __forceinline__ void dc_inner_voxel(const Fields<float>& E, const Fields<float>& E2,
+                                               const Fields<float>& R, const uint8_t* codes,
+                                               const Grid& g, int lin) {
+  int x, y, z;
+  lin_to_xyz(lin, g, x, y, z);
+  const long long px = g.px32, pl = g.pl32;
+  int code = codes[((long long)z * g.NY + y) * g.pxc + x];
+  long long c = (long long)z * pl + (long long)y * px + x;
+  Stencil<float> s;
+  gather<float, 0, true, 2>(s, E, E, c, x, y, z, g, px, pl);
+  float un, vn, wn, pn;
+  update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
+  un += __ldg(R.u + c);
+  vn += __ldg(R.v + c);
+  wn += __ldg(R.w + c);
+  pn += __ldg(R.p + c);
+  write_voxel<float, true>(E2, c, x, y, z, g, px, pl, un, vn, wn, pn);
+}
+
+// x += e at a fluid voxel and at every halo copy a sweep writes for it (the
+// only places where e can be non-zero).
+__device__ __forceinline__ void dc_correct_voxel(const Fields<double>& X, const Fields<float>& E,
+                                                 const Grid& g, int lin) {
+  int x, y, z;
+  lin_to_xyz(lin, g, x, y, z);
+  auto add = [&](int xx, int yy, int zz) {
+    long long c64 = (long long)zz * g.pl64 + (long long)yy * g.px64 + xx;
+    long long c32 = (long long)zz * g.pl32 + (long long)yy * g.px32 + xx;
+    X.u[c64] += (double)E.u[c32];
+    X.v[c64] += (double)E.v[c32];
+    X.w[c64] += (double)E.w[c32];
+    X.p[c64] += (double)E.p[c32];
+  };
+  add(x, y, z);
+  if (g.per[0]) {
+    if (x < 4) add(x + g.nx, y, z);
+    if (x >= g.nx) add(x - g.nx, y, z);
+  }
+  if (g.per[1]) {
+    if (y < 4) add(x, y + g.ny, z);
+    if (y >= g.ny) add(x, y - g.ny, z);
+  }
+  if (g.per[2]) {
+    if (z < 4) add(x, y, z + g.nz);
+    if (z >= g.nz) add(x, y, z - g.nz);
+  }
+}
+
 }  // namespace pm
