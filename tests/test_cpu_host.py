@@ -29,8 +29,8 @@ def lib():
 
 def header_symbols():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:pm_status|const char\*|double)\s+(pm_\w+)\(", src,
-                                 re.M)))
+    return sorted(set(re.findall(r"^\s*(?:pm_status|const char\*|double|uint64_t)\s+(pm_\w+)\(",
+                                 src, re.M)))
 
 
 def test_header_symbols_exported(lib):
