@@ -46,6 +46,11 @@ def parse():
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", choices=["c2", "c4", "c5"], default="c2",
+                    help="c2: 128^3 tensor workload (default); c4: batched uneven samples; "
+                         "c5: serving stream with Poisson arrivals")
+    ap.add_argument("--samples", type=int, default=64, help="c4/c5: number of requests")
+    ap.add_argument("--max-axis", type=int, default=128, help="c5: largest axis length")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                     help="run two it_eval blocks of one resident problem and exit (a small, "
                          "self-contained case for ncu captures)")
@@ -362,10 +367,157 @@ def run_profile_case(args):
     return 0
 
 
+# ------------------------------------------------------------------ serving workloads
+def c4_samples(n: int, seed: int = 4):
+    """Uneven samples: each axis from {32,48,64,96,128}; half sphere packs
+    (radii U[2,8]), half thresholded Gaussian fields (sigma U[1.5,4]); target
+    porosity U[0.15,0.5]; boundary_method 0 or 1; per-sample seeds."""
+    from poremaps_gb300 import synth
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        shape = tuple(int(v) for v in rng.choice([32, 48, 64, 96, 128], 3))
+        phi = float(rng.uniform(0.15, 0.5))
+        bc = int(rng.integers(0, 2))
+        if i % 2 == 0:
+            g = synth.sphere_pack(shape, rmin=2.0, rmax=8.0, solid_fraction=1 - phi,
+                                  seed=seed * 100003 + i)
+        else:
+            g = synth.gaussian_field(shape, float(rng.uniform(1.5, 4.0)), phi,
+                                     seed=seed * 100003 + i)
+        out.append((g, bc))
+    return out
+
+
+def c5_samples(n: int, max_axis: int, seed: int = 5):
+    """Serving stream: axes log-uniform in [32, max_axis], generators as c4,
+    porosity U[0.12,0.45], boundary_method in {0,1,2}."""
+    from poremaps_gb300 import synth
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        shape = tuple(int(round(np.exp(rng.uniform(np.log(32), np.log(max_axis))))) for _ in range(3))
+        phi = float(rng.uniform(0.12, 0.45))
+        bc = int(rng.integers(0, 3))
+        if i % 2 == 0:
+            g = synth.sphere_pack(shape, rmin=2.0, rmax=8.0, solid_fraction=1 - phi,
+                                  seed=seed * 100003 + i)
+        else:
+            g = synth.gaussian_field(shape, float(rng.uniform(1.5, 4.0)), phi,
+                                     seed=seed * 100003 + i)
+        out.append((g, bc))
+    return out
+
+
+SERVE_KW = dict(solving_algorithm=2, voxel_size=1e-5, eps=1e-6, it_eval=100, it_write=100,
+                max_iter=200000)
+
+
+def run_c4(args):
+    import poremaps_gb300 as pm
+
+    pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    t_gen = time.perf_counter()
+    reqs = c4_samples(args.samples)
+    t_gen = time.perf_counter() - t_gen
+    nvox = sum(g.size for g, _ in reqs)
+    # batched mixed-precision server
+    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1)
+    t0 = time.perf_counter()
+    tickets = {srv.submit(g, boundary_method=bc, **SERVE_KW): i for i, (g, bc) in enumerate(reqs)}
+    done = {}
+    while len(done) < len(reqs):
+        srv.step()
+        for c in srv.poll():
+            done[tickets[c.ticket]] = c
+    t_mx = time.perf_counter() - t0
+    busy, wall, lups = srv.stats()
+    srv.close()
+    # plain FP64 GPU form, one sample after another (Jacobi order, FMA form: the
+    # fastest FP64 form and the same ordering as the mixed form)
+    t0 = time.perf_counter()
+    plain = []
+    for g, bc in reqs:
+        with pm.Problem(g, None, boundary_method=bc, precision="fp64", order="jacobi",
+                        **SERVE_KW) as p:
+            plain.append(p.solve())
+    t_64 = time.perf_counter() - t0
+    rel = [max(abs(done[i].result.wk33 - r.wk33), abs(done[i].result.wk13 - r.wk13),
+               abs(done[i].result.wk23 - r.wk23)) / abs(r.wk33) for i, r in enumerate(plain)]
+    out = {"metric": "solves/h", "value": 3600.0 * len(reqs) / t_mx, "unit": "solves/h",
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": f"{len(reqs)} uneven samples (axes from {{32,48,64,96,128}}), "
+                                  "half sphere packs r U[2,8], half Gaussian sigma U[1.5,4], "
+                                  "porosity U[0.15,0.5], bc 0/1, GS, eps 1e-6",
+                      "total_voxels": nvox, "generation_s": t_gen},
+           "batched_mixed": {"solves_per_h": 3600.0 * len(reqs) / t_mx, "seconds": t_mx,
+                             "device_busy_ms": busy, "glups_busy": lups / (busy * 1e6)},
+           "plain_fp64": {"solves_per_h": 3600.0 * len(reqs) / t_64, "seconds": t_64},
+           "speedup_vs_plain_fp64": t_64 / t_mx,
+           "k_rel_err_vs_plain_fp64": {"max": max(rel), "median": float(np.median(rel))},
+           "iterations": {"min": min(c.result.sweeps for c in done.values()),
+                          "max": max(c.result.sweeps for c in done.values())}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_c5(args):
+    import poremaps_gb300 as pm
+
+    pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reqs = c5_samples(args.samples, args.max_axis)
+    # arrival rate: keep the device busy -- mean inter-arrival = 0.8 x the mean
+    # solve time measured on the first requests alone
+    rng = np.random.default_rng(55)
+    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1)
+    probe = time.perf_counter()
+    t = {srv.submit(reqs[0][0], boundary_method=reqs[0][1], **SERVE_KW): 0}
+    while srv.step():
+        pass
+    srv.poll()
+    solo = time.perf_counter() - probe
+    gaps = rng.exponential(0.8 * solo * np.mean([g.size for g, _ in reqs]) / reqs[0][0].size,
+                           len(reqs))
+    arrive = np.cumsum(gaps) - gaps[0]
+    t0 = time.perf_counter()
+    tickets, done, nxt = {}, {}, 0
+    while len(done) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and arrive[nxt] <= now:
+            g, bc = reqs[nxt]
+            tickets[srv.submit(g, boundary_method=bc, **SERVE_KW)] = nxt
+            nxt += 1
+        if srv.step() == 0 and nxt < len(reqs):
+            time.sleep(max(0.0, min(0.01, arrive[nxt] - (time.perf_counter() - t0))))
+        for c in srv.poll():
+            done[tickets[c.ticket]] = c
+    total = time.perf_counter() - t0
+    busy, wall, lups = srv.stats()
+    srv.close()
+    lat = np.array([c.finish_ms - c.submit_ms for c in done.values()]) / 1e3
+    out = {"metric": "p99 time-to-permeability", "value": float(np.percentile(lat, 99)),
+           "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f32+f64",
+           "data": "synthetic",
+           "config": {"workload": f"{len(reqs)} requests, Poisson arrivals, axes log-uniform in "
+                                  f"[32,{args.max_axis}], porosity U[0.12,0.45], bc 0/1/2, GS, "
+                                  "eps 1e-6, mixed-precision server"},
+           "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "solves_per_h": 3600.0 * len(reqs) / total,
+           "device_busy_frac": (busy / 1e3) / total}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.profile_case:
         return run_profile_case(args)
+    if args.workload == "c4":
+        return run_c4(args)
+    if args.workload == "c5":
+        return run_c5(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

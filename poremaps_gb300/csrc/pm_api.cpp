@@ -161,6 +161,13 @@ namespace {
 
 pm_status reduce_launch(pm_problem* pr, int full) {
   int mode = (pr->precision == PM_PREC_MIXED && pr->dc_pos > 0) ? 1 : 0;
+  if (pr->order == PM_ORDER_REFERENCE) {
+    CK(launch_reduce_serial(pr->F[pr->cur], full, pr->codes, pr->g, pr->prm.dom_interest,
+                            pr->dout, pr->st));
+    CK(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(double) * kRedVals, cudaMemcpyDeviceToHost,
+                       pr->st));
+    return PM_OK;
+  }
   CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
                    pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
                    pr->prm.dom_interest, pr->partials, pr->dout, pr->st));

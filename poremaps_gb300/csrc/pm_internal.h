@@ -107,6 +107,11 @@ cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full,
                           const uint8_t* codes, const Grid& g, const int di[6],
                           double* partials, double* out, cudaStream_t st);
 
+// The same sums in the reference's serial lexicographic order (bitwise equal
+// to the reference's reductions; used by the reference order).
+cudaError_t launch_reduce_serial(Fields<double> x, int full, const uint8_t* codes, const Grid& g,
+                                 const int di[6], double* out, cudaStream_t st);
+
 cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
                           const Grid& g, double* out, cudaStream_t st);
 cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st);

@@ -549,6 +549,74 @@ cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full,
   return cudaGetLastError();
 }
 
+
+// Serial-order sums for the reference order: the reference accumulates voxel
+// by voxel in lexicographic order (evaluation.cc:87-149, 231-241), so the
+// bit-exact mode does the same.  One warp loads 32 consecutive x of a row,
+// lane 0 adds them in x order (a dependent chain of adds, about 0.3 ms for a
+// 48x48x64 domain, once per it_eval sweeps).
+__global__ void k_reduce_serial(Fields<double> x, int full, const uint8_t* codes, Grid g, int d0,
+                                int d1, int d2, int d3, int d4, int d5, double* out) {
+  const int lane = threadIdx.x;
+  const bool dofi = d0 | d1 | d2 | d3 | d4 | d5;
+  double su = 0.0, sv = 0.0, sw = 0.0, mx = 0.0;
+  double bu = 0.0, bv = 0.0, bw = 0.0, p0 = 0.0, pe = 0.0;
+  for (int zp = 0; zp < g.nz; ++zp)
+    for (int yp = 0; yp < g.ny; ++yp)
+      for (int x0 = 0; x0 < g.nx; x0 += 32) {
+        int xp = x0 + lane;
+        bool fl = false;
+        double u = 0.0, v = 0.0, w = 0.0, p = 0.0;
+        if (xp < g.nx) {
+          long long cc = (long long)(zp + 2) * g.plc + (long long)(yp + 2) * g.pxc + xp + 2;
+          long long c = (long long)(zp + 2) * g.pl64 + (long long)(yp + 2) * g.px64 + xp + 2;
+          fl = codes[cc] != 0;
+          if (fl) {
+            w = x.w[c];
+            if (full) { u = x.u[c]; v = x.v[c]; p = x.p[c]; }
+          }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, fl);
+        for (int k = 0; k < 32; ++k) {
+          double wk = __shfl_sync(0xffffffffu, w, k);
+          double uk = 0.0, vk = 0.0, pk = 0.0;
+          if (full) {
+            uk = __shfl_sync(0xffffffffu, u, k);
+            vk = __shfl_sync(0xffffffffu, v, k);
+            pk = __shfl_sync(0xffffffffu, p, k);
+          }
+          if (lane == 0 && ((m >> k) & 1u)) {
+            sw += wk;
+            if (full) {
+              su += uk;
+              sv += vk;
+              if (wk > mx) mx = wk;
+              int xk = x0 + k;
+              if (dofi && !(xk < d0 || xk > d1 || yp < d2 || yp > d3 || zp < d4 || zp > d5)) {
+                bu += uk;
+                bv += vk;
+                bw += wk;
+                if (zp == d4) p0 += pk;
+                if (zp == d5) pe += pk;
+              }
+            }
+          }
+        }
+      }
+  if (lane == 0) {
+    out[0] = su; out[1] = sv; out[2] = sw; out[3] = mx;
+    out[4] = bu; out[5] = bv; out[6] = bw; out[7] = p0; out[8] = pe;
+  }
+}
+
+cudaError_t launch_reduce_serial(Fields<double> x, int full, const uint8_t* codes, const Grid& g,
+                                 const int di[6], double* out, cudaStream_t st) {
+  k_reduce_serial<<<1, 32, 0, st>>>(x, full, codes, g, di[0], di[1], di[2], di[3], di[4], di[5],
+                                    out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ export
 // Interior of a padded FP64 field into a dense x-fastest array (the layout of
 // write_output_raw, output.cc:82-91), optionally plus an FP32 correction.
