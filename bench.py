@@ -268,17 +268,22 @@ def run_gpu(args):
     lups_step = 3 * SWEEPS_PER_BLOCK * nvox
     value = world * lups_step / (ms_mx * 1e-3) / 1e9
     kernel_ms = probs_mx[2].kernel_time(0, 50)
+    kname = {0: "k_zmarch_inner 32x16 (TMA z-march FP32 correction sweep)",
+             3: "k_zmarch_inner 64x8 (TMA z-march FP32 correction sweep)",
+             1: "k_dc_inner (fluid-list FP32 correction sweep)",
+             2: "k_dc_inner_occ (fluid-list FP32 correction sweep, 4 blocks/SM)"}[
+        probs_mx[2].kernel()]
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = nvox * ALGO_BYTES_MIXED_INNER / (kernel_ms * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_dc_inner_sphere128_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "k_zmarch_inner_sphere128_traffic.json")
     if os.path.exists(tpath):
         t = json.load(open(tpath))
         traffic = t["dram_bytes_per_launch"] * nvox / t["nvox"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "k_dc_inner (FP32 correction sweep)",
+                "kernel": kname, "kernel_choice": "autotuned at problem creation",
                 "algorithmic_bytes_per_lup": ALGO_BYTES_MIXED_INNER,
                 "kernel_ms": kernel_ms,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst, of measured)" if peaks

@@ -95,6 +95,11 @@ typedef struct {
   int arith;                    /* pm_arith (FP64 sweeps) */
   int write_log;                /* 1: append the reference log rows to log_file_name */
   int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
+  int kernel;                   /* correction sweep of the mixed form: -1 autotune
+                                   (default: time every candidate on the problem, keep
+                                   the fastest), 0 TMA z-march 32x16 tiles, 3 TMA
+                                   z-march 64x8 tiles, 1 fluid-list gather, 2 fluid-list
+                                   gather at four blocks per SM */
 } pm_params;
 
 typedef struct {
@@ -168,6 +173,9 @@ pm_status pm_block_timed(pm_problem* pr, int n, int check, double* permeability,
  * (kernel 0: the form's main sweep -- the FP32 correction sweep of the mixed
  * form, the Jacobi/red-black FP64 sweep otherwise).  The state is restored. */
 pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms);
+/* The correction-sweep kernel a mixed-precision problem uses (pm_params.kernel
+ * values; the autotuned choice when it was created with kernel = -1). */
+pm_status pm_get_kernel(pm_problem* pr, int* kernel);
 /* Number of kernels this library has launched in this process. */
 uint64_t pm_kernel_launches(void);
 

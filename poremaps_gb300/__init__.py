@@ -49,7 +49,7 @@ class Params(C.Structure):
                 ("solving_algorithm", C.c_uint), ("eps", C.c_double), ("porosity", C.c_double),
                 ("dom_interest", C.c_int * 6), ("write_output", C.c_int * 4),
                 ("order", C.c_int), ("precision", C.c_int), ("arith", C.c_int),
-                ("write_log", C.c_int), ("mixed_inner", C.c_int)]
+                ("write_log", C.c_int), ("mixed_inner", C.c_int), ("kernel", C.c_int)]
 
 
 class Result(C.Structure):
@@ -80,7 +80,7 @@ EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
            "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
            "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
-           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_reduce_fields_noalloc",
+           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_reduce_fields_noalloc",
            "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms"]
@@ -124,6 +124,7 @@ def load_library(path: str = LIB_PATH):
                                      P(C.c_double)]),
         "pm_kernel_time": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double)]),
         "pm_kernel_launches": (C.c_uint64, []),
+        "pm_get_kernel": (C.c_int, [vp, P(C.c_int)]),
         "pm_reduce_fields_noalloc": (C.c_int, [P(C.c_int), vp, vp, vp, vp, vp, P(C.c_int), vp,
                                                vp]),
         "pm_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
@@ -261,6 +262,12 @@ class Problem:
         _check(load_library().pm_block_timed(self.h, n, int(check), C.byref(k), C.byref(conv),
                                              C.byref(ms)))
         return ms.value, conv.value, k.value
+
+    def kernel(self) -> int:
+        """Correction-sweep kernel in use (mixed form)."""
+        k = C.c_int()
+        _check(load_library().pm_get_kernel(self.h, C.byref(k)))
+        return k.value
 
     def kernel_time(self, kernel: int = 0, n: int = 20) -> float:
         v = C.c_double()

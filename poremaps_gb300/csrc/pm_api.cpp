@@ -86,6 +86,30 @@ pm_status validate(const pm_params* p) {
 pm_status device_sync(pm_problem* pr, const char* where) {
   cudaError_t e = cudaStreamSynchronize(pr->st);
   if (e != cudaSuccess) return cuda_error(e, where);
+  if (pr->zp) {
+    int flag = 0;
+    e = cudaMemcpy(&flag, zmarch_error_flag(pr->zp), sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, where);
+    if (flag) {
+      cudaMemset(zmarch_error_flag(pr->zp), 0, sizeof(int));
+      return set_error(PM_ERR_CUDA, "%s: a TMA pipeline wait of the z-march sweep timed out",
+                       where);
+    }
+  }
+  return PM_OK;
+}
+
+// The FP32 correction sweep e_out = L(e_in) + r of the mixed form.
+pm_status correction_sweep(pm_problem* pr, int src) {
+  if (pr->zp) {
+    CK(zmarch_inner(pr->zp, src, pr->E[1 - src], pr->g, pr->solver, pr->st));
+  } else if (pr->kern == 2) {
+    CK(launch_dc_inner_occ(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist,
+                           pr->g, pr->solver, pr->st));
+  } else {
+    CK(launch_dc_inner(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist, pr->g,
+                       pr->solver, pr->st));
+  }
   return PM_OK;
 }
 
@@ -103,6 +127,50 @@ pm_status iterate64(pm_problem* pr) {
   }
   pr->cur = 1 - pr->cur;
   return PM_OK;
+}
+
+// Correction-sweep kernels of the mixed form: 0 TMA z-march with 32 x 16
+// tiles, 3 the same with 64 x 8 tiles, 1 fluid-list gather, 2 fluid-list
+// gather compiled for four blocks per SM.  kernel < 0 times every candidate
+// on this problem (a few launches each; the correction buffers are scratch
+// until the first residual sweep) and keeps the fastest.
+pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
+  const bool tma = zmarch_available() != 0;
+  auto make = [&](int k) -> pm_status {
+    if (pr->zp) { zmarch_destroy(pr->zp); pr->zp = nullptr; }
+    pr->kern = k;
+    if (k == 0 || k == 3) {
+      CK(zmarch_create(&pr->zp, pr->g, pr->E[0], pr->E[1], pr->R, pr->codes, 0, k == 3));
+    }
+    return PM_OK;
+  };
+  if (kernel >= 0) {
+    if ((kernel == 0 || kernel == 3) && !tma) kernel = 1;
+    return make(kernel);
+  }
+  int cands[4] = {1, 2, 0, 3};
+  int nc = tma ? 4 : 2;
+  float best = 1e30f;
+  int bestk = 1;
+  for (int i = 0; i < nc; ++i) {
+    pm_status s = make(cands[i]);
+    if (s != PM_OK) return s;
+    for (int w = 0; w < 2; ++w)
+      if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
+    CK(cudaEventRecord(pr->ev0, pr->st));
+    for (int r = 0; r < 5; ++r)
+      if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
+    CK(cudaEventRecord(pr->ev1, pr->st));
+    if ((s = device_sync(pr, "kernel autotune")) != PM_OK) return s;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+    if (ms < best) { best = ms; bestk = cands[i]; }
+  }
+  pm_status s = make(bestk);
+  if (s != PM_OK) return s;
+  CK(launch_zero32(pr->E[0], pr->g, pr->st));
+  CK(launch_zero32(pr->E[1], pr->g, pr->st));
+  return device_sync(pr, "kernel autotune");
 }
 
 pm_status dc_flush(pm_problem* pr) {
@@ -124,8 +192,8 @@ pm_status iterate_mixed(pm_problem* pr) {
     CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list, pr->nlist,
                           pr->g, pr->solver, pr->st));
   } else {
-    CK(launch_dc_inner(pr->E[pr->ecur], pr->E[1 - pr->ecur], pr->R, pr->codes, pr->list,
-                       pr->nlist, pr->g, pr->solver, pr->st));
+    pm_status s = correction_sweep(pr, pr->ecur);
+    if (s != PM_OK) return s;
     pr->ecur = 1 - pr->ecur;
   }
   pr->dc_pos++;
@@ -298,6 +366,7 @@ pm_status pm_params_default(pm_params* p) {
   p->arith = PM_ARITH_FAST;
   p->write_log = 0;
   p->mixed_inner = 0;
+  p->kernel = -1;
   return PM_OK;
 }
 
@@ -377,6 +446,10 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   CKF(launch_copy_fields64(pr->F[1], pr->F[0], g, pr->st));
   CKF(cudaStreamSynchronize(pr->st));
   pr->nlist = *(int*)pr->hout;
+  if (pr->precision == PM_PREC_MIXED) {
+    pm_status ts = choose_correction_kernel(pr, p->kernel);
+    if (ts != PM_OK) return fail(ts);
+  }
   unsigned long long* hc = (unsigned long long*)((char*)pr->hout + 64);
   pr->counts = {(long long)hc[0], (long long)hc[1], (long long)hc[2], (long long)hc[3]};
   // get_porosity (geometry.cc:335-364): fluid count / interior voxel count
@@ -394,6 +467,7 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
 pm_status pm_problem_destroy(pm_problem* pr) {
   if (!pr) return PM_OK;
   if (pr->st) cudaStreamSynchronize(pr->st);
+  zmarch_destroy(pr->zp);
   cudaFree(pr->codes_base);
   cudaFree(pr->list);
   cudaFree(pr->f64_base[0]);
@@ -546,8 +620,8 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
         CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list,
                               pr->nlist, pr->g, pr->solver, pr->st));
       } else {
-        CK(launch_dc_inner(pr->E[pr->ecur], pr->E[1 - pr->ecur], pr->R, pr->codes, pr->list,
-                           pr->nlist, pr->g, pr->solver, pr->st));
+        pm_status s = correction_sweep(pr, pr->ecur);
+        if (s != PM_OK) return s;
       }
     } else {
       Fields<double> A = pr->F[pr->cur], B = pr->F[1 - pr->cur];
@@ -572,6 +646,12 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
 }
 
 uint64_t pm_kernel_launches(void) { return (uint64_t)launches_total(); }
+
+pm_status pm_get_kernel(pm_problem* pr, int* kernel) {
+  if (!pr || !kernel) return set_error(PM_ERR_INVALID, "bad arguments");
+  *kernel = pr->kern;
+  return PM_OK;
+}
 
 pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double* p) {
   if (!pr) return set_error(PM_ERR_INVALID, "bad arguments");

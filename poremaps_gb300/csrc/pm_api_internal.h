@@ -5,6 +5,7 @@
 
 #include "../../include/poremaps.h"
 #include "pm_internal.h"
+#include "pm_zmarch.h"
 
 // One device-resident domain (the state behind a pm_problem handle).
 struct pm_problem {
@@ -31,6 +32,8 @@ struct pm_problem {
   void* scratch = nullptr;  // export buffer
   size_t scratch_bytes = 0;
   int coop_blocks = 0;
+  pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
+  int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
   // state
   int cur = 0;        // FP64 state buffer holding the current iterate
   int ecur = 0;       // FP32 correction buffer holding e

@@ -102,6 +102,28 @@ __global__ void __launch_bounds__(256) k_dc_inner(Fields<float> E, Fields<float>
     dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
 }
 
+// The same sweep compiled for four resident blocks per SM (at most 64
+// registers per thread): more warps in flight to hide the gather latency.
+template <int SOLVER>
+__global__ void __launch_bounds__(256, 4) k_dc_inner_occ(Fields<float> E, Fields<float> E2,
+                                                         Fields<float> R, const uint8_t* codes,
+                                                         const int* list, int nlist, Grid g) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
+}
+
+cudaError_t launch_dc_inner_occ(Fields<float> e, Fields<float> e2, Fields<float> r,
+                                const uint8_t* codes, const int* list, int nlist, const Grid& g,
+                                int solver, cudaStream_t st) {
+  int blocks = (nlist + 255) / 256;
+  if (blocks < 1) return cudaSuccess;
+  if (solver == 1) k_dc_inner_occ<1><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  else if (solver == 2) k_dc_inner_occ<2><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  else k_dc_inner_occ<3><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
                             const uint8_t* codes, const int* list, int nlist, const Grid& g,
                             int solver, cudaStream_t st) {
@@ -123,6 +145,5 @@ cudaError_t launch_zero32(Fields<float> e, const Grid& g, cudaStream_t st) {
   return cudaMemsetAsync(e.p, 0, bytes, st);
 }
 
-int zmarch_available() { return 0; }
 
 }  // namespace pm

@@ -97,6 +97,9 @@ cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> 
 cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
                             const uint8_t* codes, const int* list, int nlist, const Grid& g,
                             int solver, cudaStream_t st);
+cudaError_t launch_dc_inner_occ(Fields<float> e, Fields<float> e2, Fields<float> r,
+                                const uint8_t* codes, const int* list, int nlist, const Grid& g,
+                                int solver, cudaStream_t st);
 cudaError_t launch_zero32(Fields<float> e, const Grid& g, cudaStream_t st);
 
 // Reductions.  mode 0: FP64 fields; mode 1: FP64 x + FP32 e.  full = 0 only
@@ -116,8 +119,5 @@ cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes,
                           const Grid& g, double* out, cudaStream_t st);
 cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st);
 
-// z-march TMA kernel for the FP32 correction sweep (dense tiles).
-struct ZmarchPlan;
-int zmarch_available();
 
 }  // namespace pm

@@ -134,6 +134,7 @@ pm_status admit(pm_server* s) {
     p.order = PM_ORDER_JACOBI;
     p.write_log = 0;
     p.mixed_inner = p.it_eval;  // corrections after iterations 0, it_eval, 2 it_eval, ...
+    p.kernel = 1;               // the batched kernels walk fluid lists
     size_t bytes = problem_device_bytes(&p);
     if (s->used + bytes > s->budget) {
       if (s->res.empty()) {  // can never fit: fail it instead of blocking the queue
