@@ -168,8 +168,8 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   }
   pm_status s = make(bestk);
   if (s != PM_OK) return s;
-  CK(launch_zero32(pr->E[0], pr->g, pr->st));
-  CK(launch_zero32(pr->E[1], pr->g, pr->st));
+  CK(launch_zero4(pr->E[0], pr->g, pr->st));
+  CK(launch_zero4(pr->E[1], pr->g, pr->st));
   return device_sync(pr, "kernel autotune");
 }
 
@@ -259,8 +259,8 @@ pm_status reset_state(pm_problem* pr) {
   CK(launch_init64(pr->F[0], pr->codes, pr->g, pr->st));
   CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
   if (pr->precision == PM_PREC_MIXED) {
-    CK(launch_zero32(pr->E[0], pr->g, pr->st));
-    CK(launch_zero32(pr->E[1], pr->g, pr->st));
+    CK(launch_zero4(pr->E[0], pr->g, pr->st));
+    CK(launch_zero4(pr->E[1], pr->g, pr->st));
   }
   pr->cur = pr->ecur = pr->dc_pos = 0;
   pr->iteration = 0;
@@ -337,7 +337,7 @@ pm_status write_log_row(const char* path, bool first, int iteration, double conv
 size_t problem_device_bytes(const pm_params* p) {
   Grid g = make_grid(p->size[0], p->size[1], p->size[2], p->boundary_method);
   size_t b = (size_t)g.allocc + 4 * (size_t)g.nvox + 2 * 4 * 8 * (size_t)g.alloc64;
-  if (p->precision == PM_PREC_MIXED) b += 3 * 4 * 4 * (size_t)g.alloc32;
+  if (p->precision == PM_PREC_MIXED) b += 3 * sizeof(float4) * (size_t)g.alloc4;
   b += 8 * (size_t)g.nvox;  // export scratch
   return b + (1 << 20);
 }
@@ -416,18 +416,13 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
                 base + 3 * g.alloc64 + kXoff64};
   }
   if (pr->precision == PM_PREC_MIXED) {
-    CKF(cudaMalloc((void**)&pr->f32_base, 12 * sizeof(float) * (size_t)g.alloc32));
-    CKF(cudaMemsetAsync(pr->f32_base, 0, 12 * sizeof(float) * (size_t)g.alloc32, pr->st));
-    float* b = pr->f32_base;
+    CKF(cudaMalloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
+    CKF(cudaMemsetAsync(pr->f32_base, 0, 3 * sizeof(float4) * (size_t)g.alloc4, pr->st));
     for (int k = 0; k < 3; ++k) {
-      Fields<float> f = {b + (4 * k) * g.alloc32 + kXoff32, b + (4 * k + 1) * g.alloc32 + kXoff32,
-                         b + (4 * k + 2) * g.alloc32 + kXoff32,
-                         b + (4 * k + 3) * g.alloc32 + kXoff32};
+      float4* f = pr->f32_base + k * g.alloc4 + kXoff4;
       if (k < 2) pr->E[k] = f;
       else pr->R = f;
     }
-  } else {
-    pr->E[0] = pr->E[1] = pr->R = {nullptr, nullptr, nullptr, nullptr};
   }
   CKF(cudaMalloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
   CKF(cudaMalloc((void**)&pr->dout, sizeof(double) * 16));
@@ -662,7 +657,7 @@ pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double*
   const double* src[4] = {f.u, f.v, f.w, f.p};
   for (int k = 0; k < 4; ++k) {
     if (!out[k]) continue;
-    CK(launch_pack64(src[k], nullptr, pr->codes, k == 3 && pr->order != PM_ORDER_REFERENCE, pr->g,
+    CK(launch_pack64(src[k], pr->codes, k == 3 && pr->order != PM_ORDER_REFERENCE, pr->g,
                      (double*)pr->scratch, pr->st));
     CK(cudaMemcpyAsync(out[k], pr->scratch, sizeof(double) * pr->g.nvox, cudaMemcpyDeviceToHost,
                        pr->st));

@@ -24,8 +24,9 @@ struct pm_problem {
   int nlist = 0;
   double* f64_base[2] = {nullptr, nullptr};
   pm::Fields<double> F[2];
-  float* f32_base = nullptr;  // e0, e1, r
-  pm::Fields<float> E[2], R;
+  float4* f32_base = nullptr;  // e0, e1, r (interleaved u, v, w, p)
+  float4* E[2] = {nullptr, nullptr};
+  float4* R = nullptr;
   double* partials = nullptr;
   double* dout = nullptr;
   double* hout = nullptr;  // pinned

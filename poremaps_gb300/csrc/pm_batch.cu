@@ -26,7 +26,7 @@ __device__ __forceinline__ void walk_items(const WorkItem* items, int nitems, F 
 __global__ void k_batch_residual(const SampleDesc* d, const WorkItem* items, int nitems) {
   walk_items(items, nitems, [&](int s, int q) {
     const SampleDesc& sd = desc_of(d, s);
-    const Fields<float>& E = sd.ecur0 ? sd.E1 : sd.E0;
+    float4* E = sd.ecur0 ? sd.E1 : sd.E0;
     int lin = sd.list[q];
     if (sd.solver == 3) dc_residual_voxel<3>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
     else if (sd.solver == 2) dc_residual_voxel<2>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
@@ -38,8 +38,8 @@ __global__ void k_batch_inner(const SampleDesc* d, const WorkItem* items, int ni
   walk_items(items, nitems, [&](int s, int q) {
     const SampleDesc& sd = desc_of(d, s);
     const int a = (sd.ecur0 + round - 1) & 1;
-    const Fields<float>& Ein = a ? sd.E1 : sd.E0;
-    const Fields<float>& Eout = a ? sd.E0 : sd.E1;
+    const float4* Ein = a ? sd.E1 : sd.E0;
+    float4* Eout = a ? sd.E0 : sd.E1;
     int lin = sd.list[q];
     if (sd.solver == 3) dc_inner_voxel<3>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
     else if (sd.solver == 2) dc_inner_voxel<2>(Ein, Eout, sd.R, sd.codes, sd.g, lin);

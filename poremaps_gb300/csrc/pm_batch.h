@@ -9,7 +9,7 @@ namespace pm {
 struct SampleDesc {
   Grid g;
   Fields<double> X0, X1;  // FP64 state (mixed form: X0 is x; FP64 form: ping-pong)
-  Fields<float> E0, E1, R;
+  float4 *E0, *E1, *R;    // interleaved FP32 correction (ping-pong) and residual
   const uint8_t* codes;
   const int* list;
   int solver;

@@ -51,22 +51,22 @@ cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* co
 
 // ------------------------------------------------------------------ mixed precision
 // x += e over the whole padded state (e is zero wherever no sweep writes).
-__global__ void k_dc_correct(Fields<double> x, Fields<float> e, Grid g) {
+__global__ void k_dc_correct(Fields<double> x, const float4* e, Grid g) {
   long long n = (long long)g.NX * g.NY * g.NZ;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
     int X = (int)(q % g.NX);
     long long r = q / g.NX;
-    long long c64 = r * g.px64 + X, c32 = r * g.px32 + X;
-    x.u[c64] += (double)e.u[c32];
-    x.v[c64] += (double)e.v[c32];
-    x.w[c64] += (double)e.w[c32];
-    x.p[c64] += (double)e.p[c32];
+    long long c64 = r * g.px64 + X, c4 = r * g.px4 + X;
+    const float4 v = e[c4];
+    x.u[c64] += (double)v.x;
+    x.v[c64] += (double)v.y;
+    x.w[c64] += (double)v.z;
+    x.p[c64] += (double)v.w;
   }
 }
 
-cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
-                              cudaStream_t st) {
+cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st) {
   k_dc_correct<<<1184, 256, 0, st>>>(x, e, g);
   count_launches(1);
   return cudaGetLastError();
@@ -74,16 +74,16 @@ cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
 
 // r = F(x) - x in FP64 (stored FP32) and the first correction e1 = r.
 template <int SOLVER>
-__global__ void __launch_bounds__(256) k_dc_residual(Fields<double> X, Fields<float> R,
-                                                     Fields<float> E, const uint8_t* codes,
-                                                     const int* list, int nlist, Grid g) {
+__global__ void __launch_bounds__(256) k_dc_residual(Fields<double> X, float4* R, float4* E,
+                                                     const uint8_t* codes, const int* list,
+                                                     int nlist, Grid g) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
     dc_residual_voxel<SOLVER>(X, R, E, codes, g, list[q]);
 }
 
-cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> e,
-                               const uint8_t* codes, const int* list, int nlist, const Grid& g,
-                               int solver, cudaStream_t st) {
+cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
+                               const int* list, int nlist, const Grid& g, int solver,
+                               cudaStream_t st) {
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
   if (solver == 1) k_dc_residual<1><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
@@ -93,11 +93,11 @@ cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> 
   return cudaGetLastError();
 }
 
-// e2 = L(e) + r over the fluid list (FP32).
+// e2 = L(e) + r over the fluid list (FP32, interleaved fields).
 template <int SOLVER>
-__global__ void __launch_bounds__(256) k_dc_inner(Fields<float> E, Fields<float> E2,
-                                                  Fields<float> R, const uint8_t* codes,
-                                                  const int* list, int nlist, Grid g) {
+__global__ void __launch_bounds__(256) k_dc_inner(const float4* E, float4* E2, const float4* R,
+                                                  const uint8_t* codes, const int* list,
+                                                  int nlist, Grid g) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
     dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
 }
@@ -105,14 +105,14 @@ __global__ void __launch_bounds__(256) k_dc_inner(Fields<float> E, Fields<float>
 // The same sweep compiled for four resident blocks per SM (at most 64
 // registers per thread): more warps in flight to hide the gather latency.
 template <int SOLVER>
-__global__ void __launch_bounds__(256, 4) k_dc_inner_occ(Fields<float> E, Fields<float> E2,
-                                                         Fields<float> R, const uint8_t* codes,
+__global__ void __launch_bounds__(256, 4) k_dc_inner_occ(const float4* E, float4* E2,
+                                                         const float4* R, const uint8_t* codes,
                                                          const int* list, int nlist, Grid g) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
     dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
 }
 
-cudaError_t launch_dc_inner_occ(Fields<float> e, Fields<float> e2, Fields<float> r,
+cudaError_t launch_dc_inner_occ(const float4* e, float4* e2, const float4* r,
                                 const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                 int solver, cudaStream_t st) {
   int blocks = (nlist + 255) / 256;
@@ -124,9 +124,9 @@ cudaError_t launch_dc_inner_occ(Fields<float> e, Fields<float> e2, Fields<float>
   return cudaGetLastError();
 }
 
-cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
-                            const uint8_t* codes, const int* list, int nlist, const Grid& g,
-                            int solver, cudaStream_t st) {
+cudaError_t launch_dc_inner(const float4* e, float4* e2, const float4* r, const uint8_t* codes,
+                            const int* list, int nlist, const Grid& g, int solver,
+                            cudaStream_t st) {
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
   if (solver == 1) k_dc_inner<1><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
@@ -136,14 +136,8 @@ cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
   return cudaGetLastError();
 }
 
-cudaError_t launch_zero32(Fields<float> e, const Grid& g, cudaStream_t st) {
-  size_t bytes = sizeof(float) * (size_t)g.pl32 * g.NZ;
-  cudaError_t err;
-  if ((err = cudaMemsetAsync(e.u, 0, bytes, st))) return err;
-  if ((err = cudaMemsetAsync(e.v, 0, bytes, st))) return err;
-  if ((err = cudaMemsetAsync(e.w, 0, bytes, st))) return err;
-  return cudaMemsetAsync(e.p, 0, bytes, st);
+cudaError_t launch_zero4(float4* e, const Grid& g, cudaStream_t st) {
+  return cudaMemsetAsync(e, 0, sizeof(float4) * (size_t)g.pl4 * g.NZ, st);
 }
-
 
 }  // namespace pm

@@ -21,14 +21,17 @@ constexpr double kDt = 1.0e-4;
 constexpr int kXoff64 = 14;
 constexpr int kXoff32 = 30;
 constexpr int kXoffC = 14;
+// The mixed form stores its FP32 correction and residual interleaved, one
+// float4 (u, v, w, p) per voxel: a stencil point is one 128-bit load.
+constexpr int kXoff4 = 6;
 
 struct Grid {
   int nx, ny, nz;
   int NX, NY, NZ;
   int per[3];          // periodic axes (x, y, z) from boundary_method
-  int px64, px32, pxc; // row pitches in elements
-  long long pl64, pl32, plc; // plane strides in elements
-  long long alloc64, alloc32, allocc; // elements to allocate (including XOFF)
+  int px64, px32, pxc, px4; // row pitches in elements
+  long long pl64, pl32, plc, pl4; // plane strides in elements
+  long long alloc64, alloc32, allocc, alloc4; // elements to allocate (including XOFF)
   long long nvox;      // nx*ny*nz
 };
 
@@ -88,25 +91,24 @@ cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* co
                            int phase, cudaStream_t st);
 
 // Mixed precision (defect correction).  x: FP64 state, e: FP32 correction
-// (ping-pong), r: FP32 residual.
-cudaError_t launch_dc_correct(Fields<double> x, Fields<float> e, const Grid& g,
-                              cudaStream_t st);
-cudaError_t launch_dc_residual(Fields<double> x, Fields<float> r, Fields<float> e,
-                               const uint8_t* codes, const int* list, int nlist,
-                               const Grid& g, int solver, cudaStream_t st);
-cudaError_t launch_dc_inner(Fields<float> e, Fields<float> e2, Fields<float> r,
-                            const uint8_t* codes, const int* list, int nlist, const Grid& g,
-                            int solver, cudaStream_t st);
-cudaError_t launch_dc_inner_occ(Fields<float> e, Fields<float> e2, Fields<float> r,
+// (ping-pong), r: FP32 residual; e and r interleaved (float4 u, v, w, p).
+cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st);
+cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
+                               const int* list, int nlist, const Grid& g, int solver,
+                               cudaStream_t st);
+cudaError_t launch_dc_inner(const float4* e, float4* e2, const float4* r, const uint8_t* codes,
+                            const int* list, int nlist, const Grid& g, int solver,
+                            cudaStream_t st);
+cudaError_t launch_dc_inner_occ(const float4* e, float4* e2, const float4* r,
                                 const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                 int solver, cudaStream_t st);
-cudaError_t launch_zero32(Fields<float> e, const Grid& g, cudaStream_t st);
+cudaError_t launch_zero4(float4* e, const Grid& g, cudaStream_t st);
 
 // Reductions.  mode 0: FP64 fields; mode 1: FP64 x + FP32 e.  full = 0 only
 // sums w.  partials: kRedBlocks*kRedVals doubles; out: kRedVals doubles.
 // implied3: the state stores swept pressure on the last interior plane and the
 // reapplied 3 is implied there (out-of-place orderings).
-cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full, int implied3,
+cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
                           const uint8_t* codes, const Grid& g, const int di[6],
                           double* partials, double* out, cudaStream_t st);
 
@@ -115,8 +117,8 @@ cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full,
 cudaError_t launch_reduce_serial(Fields<double> x, int full, const uint8_t* codes, const Grid& g,
                                  const int di[6], double* out, cudaStream_t st);
 
-cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
-                          const Grid& g, double* out, cudaStream_t st);
+cudaError_t launch_pack64(const double* f, const uint8_t* codes, int implied3, const Grid& g,
+                          double* out, cudaStream_t st);
 cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st);
 
 

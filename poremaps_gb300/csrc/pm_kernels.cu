@@ -28,6 +28,9 @@ Grid make_grid(int nx, int ny, int nz, int bm) {
   g.px64 = (int)up(kXoff64 + g.NX, 16);
   g.px32 = (int)up(kXoff32 + g.NX, 32);
   g.pxc = (int)up(kXoffC + g.NX, 16);
+  g.px4 = (int)up(kXoff4 + g.NX, 8);
+  g.pl4 = (long long)g.px4 * g.NY;
+  g.alloc4 = g.pl4 * g.NZ + 16;
   g.pl64 = (long long)g.px64 * g.NY;
   g.pl32 = (long long)g.px32 * g.NY;
   g.plc = (long long)g.pxc * g.NY;
@@ -465,7 +468,7 @@ cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* cod
 // compute_convergence / compute_permeability sums (evaluation.cc:54-262) with
 // a fixed grid and a fixed combination tree (bitwise reproducible).
 template <int MODE>
-__global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, Fields<float> e,
+__global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, const float4* e,
                                                         int full, int implied3,
                                                         const uint8_t* codes, Grid g,
                                                         int d0, int d1, int d2, int d3, int d4,
@@ -481,13 +484,15 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, Fields
     int X = xp + 2, Y = yp + 2, Z = zp + 2;
     if (!codes[((long long)Z * g.NY + Y) * g.pxc + X]) continue;
     long long c = (long long)Z * g.pl64 + (long long)Y * g.px64 + X;
-    long long c32 = (long long)Z * g.pl32 + (long long)Y * g.px32 + X;
+    long long c4 = (long long)Z * g.pl4 + (long long)Y * g.px4 + X;
+    float4 ev = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (MODE == 1) ev = e[c4];
     double w = x.w[c];
-    if (MODE == 1) w += (double)e.w[c32];
+    if (MODE == 1) w += (double)ev.z;
     acc[2] += w;
     if (!full) continue;
     double u = x.u[c], v = x.v[c];
-    if (MODE == 1) { u += (double)e.u[c32]; v += (double)e.v[c32]; }
+    if (MODE == 1) { u += (double)ev.x; v += (double)ev.y; }
     acc[0] += u;
     acc[1] += v;
     if (w > acc[3]) acc[3] = w;
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, Fields
     acc[5] += v;
     acc[6] += w;
     double p = x.p[c];
-    if (MODE == 1) p += (double)e.p[c32];
+    if (MODE == 1) p += (double)ev.w;
     if (implied3 && zp == g.nz - 1) p = 3.0;
     if (zp == d4) acc[7] += p;
     if (zp == d5) acc[8] += p;
@@ -535,7 +540,7 @@ __global__ void k_reduce_final(const double* partials, double* out) {
   }
 }
 
-cudaError_t launch_reduce(Fields<double> x, Fields<float> e, int mode, int full, int implied3,
+cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
                           const uint8_t* codes, const Grid& g, const int di[6], double* partials,
                           double* out, cudaStream_t st) {
   if (mode == 0)
@@ -622,15 +627,14 @@ cudaError_t launch_reduce_serial(Fields<double> x, int full, const uint8_t* code
 // write_output_raw, output.cc:82-91), optionally plus an FP32 correction.
 // With implied3, fluid voxels of the last interior plane export the
 // reapplied pressure 3 (the out-of-place orderings store the swept value).
-__global__ void k_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
-                         Grid g, double* out) {
+__global__ void k_pack64(const double* f, const uint8_t* codes, int implied3, Grid g,
+                         double* out) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;
        q += (long long)gridDim.x * blockDim.x) {
     int x = (int)(q % g.nx);
     long long r = q / g.nx;
     int y = (int)(r % g.ny), z = (int)(r / g.ny);
     double v = f[(long long)(z + 2) * g.pl64 + (long long)(y + 2) * g.px64 + x + 2];
-    if (e) v += (double)e[(long long)(z + 2) * g.pl32 + (long long)(y + 2) * g.px32 + x + 2];
     if (implied3 && z == g.nz - 1 &&
         codes[(long long)(z + 2) * g.plc + (long long)(y + 2) * g.pxc + x + 2])
       v = 3.0;
@@ -638,9 +642,9 @@ __global__ void k_pack64(const double* f, const float* e, const uint8_t* codes, 
   }
 }
 
-cudaError_t launch_pack64(const double* f, const float* e, const uint8_t* codes, int implied3,
-                          const Grid& g, double* out, cudaStream_t st) {
-  k_pack64<<<1184, 256, 0, st>>>(f, e, codes, implied3, g, out);
+cudaError_t launch_pack64(const double* f, const uint8_t* codes, int implied3, const Grid& g,
+                          double* out, cudaStream_t st) {
+  k_pack64<<<1184, 256, 0, st>>>(f, codes, implied3, g, out);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -285,13 +285,60 @@ __device__ __forceinline__ void sweep64_voxel(const Fields<double>& A, const Fie
   write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
 }
 
+// ---- interleaved FP32 correction fields (float4 u, v, w, p per voxel)
+
+// The stencil of one voxel from the correction: the union of its offsets is
+// 13 points, each one 128-bit load.  The voxel's own pressure on the last
+// interior plane is the reapplied (fixed) value, whose correction is 0.
+__device__ __forceinline__ void gather4(Stencil<float>& s, const float4* E, long long c, int z,
+                                        const Grid& g) {
+  const long long px = g.px4, pl = g.pl4;
+  const float4 C = __ldg(E + c);
+  const float4 XM = __ldg(E + c - 1), XP = __ldg(E + c + 1);
+  const float4 XMM = __ldg(E + c - 2), XPP = __ldg(E + c + 2);
+  const float4 YM = __ldg(E + c - px), YP = __ldg(E + c + px);
+  const float4 YMM = __ldg(E + c - 2 * px), YPP = __ldg(E + c + 2 * px);
+  const float4 ZM = __ldg(E + c - pl), ZP = __ldg(E + c + pl);
+  const float4 ZMM = __ldg(E + c - 2 * pl), ZPP = __ldg(E + c + 2 * pl);
+  s.uc = C.x; s.uxm = XM.x; s.uxp = XP.x; s.uym = YM.x; s.uyp = YP.x;
+  s.uymm = YMM.x; s.uypp = YPP.x; s.uzm = ZM.x; s.uzp = ZP.x; s.uzmm = ZMM.x; s.uzpp = ZPP.x;
+  s.vc = C.y; s.vxm = XM.y; s.vxp = XP.y; s.vxmm = XMM.y; s.vxpp = XPP.y; s.vym = YM.y;
+  s.vyp = YP.y; s.vzm = ZM.y; s.vzp = ZP.y; s.vzmm = ZMM.y; s.vzpp = ZPP.y;
+  s.wc = C.z; s.wxm = XM.z; s.wxp = XP.z; s.wxmm = XMM.z; s.wxpp = XPP.z; s.wym = YM.z;
+  s.wyp = YP.z; s.wymm = YMM.z; s.wypp = YPP.z; s.wzm = ZM.z; s.wzp = ZP.z;
+  s.pc = (z == g.NZ - 3) ? 0.f : C.w;
+  s.pxm = XM.w; s.pym = YM.w; s.pzm = ZM.w;
+}
+
+// write_voxel for the interleaved correction (homogeneous boundary values).
+__device__ __forceinline__ void write_voxel4(float4* B, long long c, int x, int y, int z,
+                                             const Grid& g, float un, float vn, float wn,
+                                             float pn) {
+  const long long px = g.px4, pl = g.pl4;
+  const float4 val = make_float4(un, vn, wn, pn);
+  B[c] = val;
+  if (g.per[0]) {
+    if (x < 4) B[c + g.nx] = val;
+    if (x >= g.nx) B[c - g.nx] = val;
+  }
+  if (g.per[1]) {
+    if (y < 4) B[c + (long long)g.ny * px] = val;
+    if (y >= g.ny) B[c - (long long)g.ny * px] = val;
+  }
+  if (g.per[2]) {
+    // the z copies landing on planes NZ-2 and 1 hold reapplied pressure: 0
+    if (z < 4) B[c + (long long)g.nz * pl] = make_float4(un, vn, wn, z == 2 ? 0.f : pn);
+    if (z >= g.nz)
+      B[c - (long long)g.nz * pl] = make_float4(un, vn, wn, z == g.nz + 1 ? 0.f : pn);
+  }
+}
+
 // r = F(x) - x (FP64, stored FP32) and the first correction e1 = r.  On the
 // last interior plane the state stores the swept pressure (the reapplied 3 is
 // implied), so its residual is taken against that stored value.
 template <int SOLVER>
-__device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, const Fields<float>& R,
-                                                  const Fields<float>& E, const uint8_t* codes,
-                                                  const Grid& g, int lin) {
+__device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, float4* R, float4* E,
+                                                  const uint8_t* codes, const Grid& g, int lin) {
   int x, y, z;
   lin_to_xyz(lin, g, x, y, z);
   int code = codes[((long long)z * g.NY + y) * g.pxc + x];
@@ -303,48 +350,40 @@ __device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, const
   const double pstored = (z == g.NZ - 3) ? __ldg(X.p + c) : s.pc;
   float ru = (float)(un - s.uc), rv = (float)(vn - s.vc), rw = (float)(wn - s.wc),
         rp = (float)(pn - pstored);
-  long long c32 = (long long)z * g.pl32 + (long long)y * g.px32 + x;
-  R.u[c32] = ru;
-  R.v[c32] = rv;
-  R.w[c32] = rw;
-  R.p[c32] = rp;
-  write_voxel<float, true>(E, c32, x, y, z, g, g.px32, g.pl32, ru, rv, rw, rp);
+  long long c4 = (long long)z * g.pl4 + (long long)y * g.px4 + x;
+  R[c4] = make_float4(ru, rv, rw, rp);
+  write_voxel4(E, c4, x, y, z, g, ru, rv, rw, rp);
 }
 
 // e2 = L(e) + r (FP32 correction sweep).
 template <int SOLVER>
-__device__ __forceinline__ void dc_inner_voxel(const Fields<float>& E, const Fields<float>& E2,
-                                               const Fields<float>& R, const uint8_t* codes,
-                                               const Grid& g, int lin) {
+__device__ __forceinline__ void dc_inner_voxel(const float4* E, float4* E2, const float4* R,
+                                               const uint8_t* codes, const Grid& g, int lin) {
   int x, y, z;
   lin_to_xyz(lin, g, x, y, z);
-  const long long px = g.px32, pl = g.pl32;
   int code = codes[((long long)z * g.NY + y) * g.pxc + x];
-  long long c = (long long)z * pl + (long long)y * px + x;
+  long long c = (long long)z * g.pl4 + (long long)y * g.px4 + x;
   Stencil<float> s;
-  gather<float, 0, true, 2>(s, E, E, c, x, y, z, g, px, pl);
+  gather4(s, E, c, z, g);
   float un, vn, wn, pn;
   update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
-  un += __ldg(R.u + c);
-  vn += __ldg(R.v + c);
-  wn += __ldg(R.w + c);
-  pn += __ldg(R.p + c);
-  write_voxel<float, true>(E2, c, x, y, z, g, px, pl, un, vn, wn, pn);
+  const float4 r = __ldg(R + c);
+  write_voxel4(E2, c, x, y, z, g, un + r.x, vn + r.y, wn + r.z, pn + r.w);
 }
 
 // x += e at a fluid voxel and at every halo copy a sweep writes for it (the
 // only places where e can be non-zero).
-__device__ __forceinline__ void dc_correct_voxel(const Fields<double>& X, const Fields<float>& E,
+__device__ __forceinline__ void dc_correct_voxel(const Fields<double>& X, const float4* E,
                                                  const Grid& g, int lin) {
   int x, y, z;
   lin_to_xyz(lin, g, x, y, z);
   auto add = [&](int xx, int yy, int zz) {
     long long c64 = (long long)zz * g.pl64 + (long long)yy * g.px64 + xx;
-    long long c32 = (long long)zz * g.pl32 + (long long)yy * g.px32 + xx;
-    X.u[c64] += (double)E.u[c32];
-    X.v[c64] += (double)E.v[c32];
-    X.w[c64] += (double)E.w[c32];
-    X.p[c64] += (double)E.p[c32];
+    const float4 e = E[(long long)zz * g.pl4 + (long long)yy * g.px4 + xx];
+    X.u[c64] += (double)e.x;
+    X.v[c64] += (double)e.y;
+    X.w[c64] += (double)e.z;
+    X.p[c64] += (double)e.w;
   };
   add(x, y, z);
   if (g.per[0]) {

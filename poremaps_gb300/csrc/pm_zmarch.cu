@@ -7,8 +7,10 @@
 // mbarrier per pipeline stage counts the bytes), prefetched D planes ahead;
 // every thread then reads its stencil from shared memory and writes the new
 // correction straight to global memory (the other ping-pong buffer, so reads
-// and writes never alias).  Ring depths follow the stencil reach: u, v need
-// planes z-2..z+2, w z-1..z+1, p z-1..z, r and the codes plane z.
+// and writes never alias).  The correction is interleaved (float4 u, v, w, p
+// per voxel): one box per plane, planes z-2..z+2 resident plus D prefetched;
+// the residual and the codes are needed for plane z only.  Each plane's fluid
+// voxels are compacted into a shared list so computing lanes are full.
 //
 // Every mbarrier wait is bounded (clock64 budget); on expiry the CTA records
 // an error code, drains its own copies still in flight (again bounded) and
@@ -23,45 +25,39 @@ namespace pm {
 
 namespace {
 
-constexpr int VX = 2;
 constexpr int D = 2;  // prefetch depth (planes)
-constexpr int NU = 5 + D, NW = 3 + D, NP = 2 + D, NR = 1 + D;
+constexpr int NE = 5 + D, NR = 1 + D;
 
-// Tile geometry: TX x TY interior columns; the x halo starts on a 16-byte
-// boundary (HX = TX + 8), the y halo is the stencil's 2 rows on each side.
+// Tile geometry: TX x TY interior columns, the stencil's 2-voxel halo on each
+// side in x and y; one float4 (u, v, w, p) per voxel, so any x start is
+// 16-byte aligned and one TMA box carries all four fields of a plane.
 template <int TX_, int TY_>
 struct Tile {
   static constexpr int TX = TX_, TY = TY_;
-  static constexpr int HX = TX + 8, HY = TY + 4;
-  static constexpr int PLANE_F = HX * HY;  // floats per halo plane of one field
-  static constexpr int TILE_F = TX * TY;   // floats per interior tile of one field
-  static constexpr int THREADS = (TX / VX) * TY;
-  static constexpr unsigned BYTES_PLANE = PLANE_F * 4, BYTES_TILE = TILE_F * 4;
-  static constexpr unsigned BYTES_CODES = TILE_F;
-  static constexpr unsigned BYTES_GROUP = 4 * BYTES_PLANE + 4 * BYTES_TILE + BYTES_CODES;
-  static constexpr unsigned BYTES_PRO = (4 + 4 + 2 + 1) * BYTES_PLANE;  // u,v 4, w 2, p 1
+  static constexpr int HX = TX + 4, HY = TY + 4;
+  static constexpr int PLANE = HX * HY;  // float4 per halo plane
+  static constexpr int TILE = TX * TY;   // voxels per interior tile
+  static constexpr int THREADS = TILE / 2;  // two columns per thread
+  static constexpr unsigned BYTES_PLANE = PLANE * 16, BYTES_TILE = TILE * 16;
+  static constexpr unsigned BYTES_GROUP = BYTES_PLANE + BYTES_TILE + TILE;
+  static constexpr unsigned BYTES_PRO = 4 * BYTES_PLANE;  // planes z0-2 .. z0+1
 };
 
 template <class T>
 struct Smem {
-  static constexpr int PLANE_F = T::PLANE_F, TILE_F = T::TILE_F, THREADS = T::THREADS;
-  float u[NU][PLANE_F];
-  float v[NU][PLANE_F];
-  float w[NW][PLANE_F];
-  float p[NP][PLANE_F];
-  float r[NR][4][TILE_F];
-  uint8_t codes[NR][TILE_F];
+  float4 e[NE][T::PLANE];
+  float4 r[NR][T::TILE];
+  uint8_t codes[NR][T::TILE];
   unsigned long long bar[NR];
   unsigned long long bar_pro;
-  unsigned short list[TILE_F];  // fluid voxels of the current plane (tile offsets)
-  int warp_count[THREADS / 32];
-  static_assert(sizeof(float) * PLANE_F % 128 == 0, "TMA slots must stay 128-byte aligned");
-  static_assert(sizeof(float) * TILE_F % 128 == 0, "TMA slots must stay 128-byte aligned");
-  static_assert(TILE_F % 128 == 0, "code slots must stay 128-byte aligned");
+  unsigned short list[T::TILE];  // fluid voxels of the current plane (tile offsets)
+  int warp_count[T::THREADS / 32];
+  static_assert(T::PLANE * 16 % 128 == 0, "TMA slots must stay 128-byte aligned");
+  static_assert(T::TILE % 128 == 0, "code slots must stay 128-byte aligned");
 };
 
 using TileA = Tile<32, 16>;
-using TileB = Tile<64, 8>;
+using TileB = Tile<32, 8>;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -108,17 +104,16 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
 }
 
 struct Maps {
-  CUtensorMap e[4];  // source correction u, v, w, p (halo boxes)
-  CUtensorMap r[4];  // residual (interior boxes)
-  CUtensorMap codes; // voxel codes (interior boxes)
+  CUtensorMap e;      // source correction (halo boxes), float4 viewed as 4 floats
+  CUtensorMap r;      // residual (interior boxes)
+  CUtensorMap codes;  // voxel codes (interior boxes)
 };
 
 template <class T, int SOLVER>
-__global__ void __launch_bounds__(T::THREADS, 2)
-    k_zmarch_inner(const __grid_constant__ Maps maps, Fields<float> E2, Grid g, int zchunk,
+__global__ void __launch_bounds__(T::THREADS)
+    k_zmarch_inner(const __grid_constant__ Maps maps, float4* E2, Grid g, int zchunk,
                    long long budget, int* err) {
   constexpr int TX = T::TX, TY = T::TY, HX = T::HX, THREADS = T::THREADS;
-  constexpr unsigned BYTES_GROUP = T::BYTES_GROUP, BYTES_PRO = T::BYTES_PRO;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem<T>& S = *reinterpret_cast<Smem<T>*>(smem_raw);
   const int bx = blockIdx.x, by = blockIdx.y;
@@ -126,21 +121,20 @@ __global__ void __launch_bounds__(T::THREADS, 2)
   const int z1 = min(z0 + zchunk, g.NZ - 2);
   if (z0 >= z1) return;
   const int L = z1 - z0;
-  const int xe = kXoff32 - 2 + bx * TX;  // halo box start: padded x = bx*TX - 2
-  const int ye = by * TY;                          // halo box start: padded y = by*TY
-  const int xr = kXoff32 + 2 + bx * TX, yr = 2 + by * TY;
+  // TMA coordinates in floats (x) / rows (y) / planes (z); one float4 = 4 floats
+  const int xe = 4 * (kXoff4 + bx * TX);      // halo box: padded x from bx*TX
+  const int ye = by * TY;                     // halo box: padded y from by*TY
+  const int xr = 4 * (kXoff4 + 2 + bx * TX);  // interior box
+  const int yr = 2 + by * TY;
   const int xc = kXoffC + 2 + bx * TX;
   const bool leader = threadIdx.x == 0;
 
   auto issue_group = [&](int j) {  // loads needed first by compute step j
     const int z = z0 + j;
     unsigned long long* b = &S.bar[j % NR];
-    mbar_expect(b, BYTES_GROUP);
-    tma_load3(S.u[(j + 4) % NU], &maps.e[0], xe, ye, z + 2, b);
-    tma_load3(S.v[(j + 4) % NU], &maps.e[1], xe, ye, z + 2, b);
-    tma_load3(S.w[(j + 2) % NW], &maps.e[2], xe, ye, z + 1, b);
-    tma_load3(S.p[(j + 1) % NP], &maps.e[3], xe, ye, z, b);
-    for (int f = 0; f < 4; ++f) tma_load3(S.r[j % NR][f], &maps.r[f], xr, yr, z, b);
+    mbar_expect(b, T::BYTES_GROUP);
+    tma_load3(S.e[(j + 4) % NE], &maps.e, xe, ye, z + 2, b);
+    tma_load3(S.r[j % NR], &maps.r, xr, yr, z, b);
     tma_load3(S.codes[j % NR], &maps.codes, xc, yr, z, b);
   };
 
@@ -151,24 +145,18 @@ __global__ void __launch_bounds__(T::THREADS, 2)
   }
   __syncthreads();
   if (leader) {
-    // prologue: u, v planes z0-2..z0+1 (slots 0..3), w z0-1, z0 (slots 0, 1), p z0-1 (slot 0)
-    mbar_expect(&S.bar_pro, BYTES_PRO);
-    for (int k = 0; k < 4; ++k) {
-      tma_load3(S.u[k], &maps.e[0], xe, ye, z0 - 2 + k, &S.bar_pro);
-      tma_load3(S.v[k], &maps.e[1], xe, ye, z0 - 2 + k, &S.bar_pro);
-    }
-    tma_load3(S.w[0], &maps.e[2], xe, ye, z0 - 1, &S.bar_pro);
-    tma_load3(S.w[1], &maps.e[2], xe, ye, z0, &S.bar_pro);
-    tma_load3(S.p[0], &maps.e[3], xe, ye, z0 - 1, &S.bar_pro);
+    // prologue: planes z0-2 .. z0+1 into slots 0..3 (plane z0-2 is slot 0)
+    mbar_expect(&S.bar_pro, T::BYTES_PRO);
+    for (int k = 0; k < 4; ++k) tma_load3(S.e[k], &maps.e, xe, ye, z0 - 2 + k, &S.bar_pro);
     for (int j = 0; j < D + 1 && j < L; ++j) issue_group(j);
   }
   int issued = min(D + 1, L);
   int waited = 0;  // groups whose barrier phase every thread has observed
   bool ok = __syncthreads_and(mbar_wait(&S.bar_pro, 0, budget));
 
-  const int tx = threadIdx.x % (TX / VX), ty = threadIdx.x / (TX / VX);
+  const int tx = threadIdx.x % (TX / 2), ty = threadIdx.x / (TX / 2);
   const int yp = by * TY + ty;  // interior y
-  const long long px = g.px32, pl = g.pl32;
+  const long long px = g.px4, pl = g.pl4;
 
   for (int j = 0; j < L && ok; ++j) {
     ok = __syncthreads_and(mbar_wait(&S.bar[j % NR], (j / NR) & 1, budget));
@@ -177,12 +165,12 @@ __global__ void __launch_bounds__(T::THREADS, 2)
     const int z = z0 + j;
     const int sr = j % NR;
     // compact the fluid voxels of this plane so that every computing lane has one
-    unsigned fl[VX];
+    unsigned fl[2];
     int nmine = 0;
 #pragma unroll
-    for (int q = 0; q < VX; ++q) {
-      const int xp = bx * TX + tx * VX + q;
-      fl[q] = (xp < g.nx && yp < g.ny && S.codes[sr][ty * TX + tx * VX + q]) ? 1u : 0u;
+    for (int q = 0; q < 2; ++q) {
+      const int xp = bx * TX + tx * 2 + q;
+      fl[q] = (xp < g.nx && yp < g.ny && S.codes[sr][ty * TX + tx * 2 + q]) ? 1u : 0u;
       nmine += fl[q];
     }
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -203,53 +191,37 @@ __global__ void __launch_bounds__(T::THREADS, 2)
     }
     int pos = base + pre - nmine;
 #pragma unroll
-    for (int q = 0; q < VX; ++q)
-      if (fl[q]) S.list[pos++] = (unsigned short)(ty * TX + tx * VX + q);
+    for (int q = 0; q < 2; ++q)
+      if (fl[q]) S.list[pos++] = (unsigned short)(ty * TX + tx * 2 + q);
     __syncthreads();
-    // plane pointers of the rings for this step
-    const float* up[5];
-    const float* vp[5];
+    const float4* P[5];  // planes z-2 .. z+2
 #pragma unroll
-    for (int d = 0; d < 5; ++d) {
-      up[d] = S.u[(j + d) % NU];  // plane z-2+d (plane z0-2 is slot 0)
-      vp[d] = S.v[(j + d) % NU];
-    }
-    const float* wp[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) wp[d] = S.w[(j + d) % NW];  // plane z-1+d
-    const float* pzm = S.p[j % NP];                         // plane z-1
-    const float* pc = S.p[(j + 1) % NP];                    // plane z
-    const float* rr[4] = {S.r[sr][0], S.r[sr][1], S.r[sr][2], S.r[sr][3]};
+    for (int d = 0; d < 5; ++d) P[d] = S.e[(j + d) % NE];
     for (int k = threadIdx.x; k < nfl; k += THREADS) {
       const int t = S.list[k];
       const int ly = t / TX, lx = t - ly * TX;
       const int code = S.codes[sr][t];
-      const int c0 = (ly + 2) * HX + lx + 4;  // centre in the halo planes
+      const int c0 = (ly + 2) * HX + lx + 2;  // centre in the halo planes
+      const float4 C = P[2][c0];
+      const float4 XM = P[2][c0 - 1], XP = P[2][c0 + 1], XMM = P[2][c0 - 2], XPP = P[2][c0 + 2];
+      const float4 YM = P[2][c0 - HX], YP = P[2][c0 + HX];
+      const float4 YMM = P[2][c0 - 2 * HX], YPP = P[2][c0 + 2 * HX];
+      const float4 ZM = P[1][c0], ZP = P[3][c0], ZMM = P[0][c0], ZPP = P[4][c0];
       Stencil<float> s;
-      s.uc = up[2][c0]; s.uxm = up[2][c0 - 1]; s.uxp = up[2][c0 + 1];
-      s.uym = up[2][c0 - HX]; s.uyp = up[2][c0 + HX];
-      s.uymm = up[2][c0 - 2 * HX]; s.uypp = up[2][c0 + 2 * HX];
-      s.uzm = up[1][c0]; s.uzp = up[3][c0]; s.uzmm = up[0][c0]; s.uzpp = up[4][c0];
-      s.vc = vp[2][c0]; s.vxm = vp[2][c0 - 1]; s.vxp = vp[2][c0 + 1];
-      s.vxmm = vp[2][c0 - 2]; s.vxpp = vp[2][c0 + 2];
-      s.vym = vp[2][c0 - HX]; s.vyp = vp[2][c0 + HX];
-      s.vzm = vp[1][c0]; s.vzp = vp[3][c0]; s.vzmm = vp[0][c0]; s.vzpp = vp[4][c0];
-      s.wc = wp[1][c0]; s.wxm = wp[1][c0 - 1]; s.wxp = wp[1][c0 + 1];
-      s.wxmm = wp[1][c0 - 2]; s.wxpp = wp[1][c0 + 2];
-      s.wym = wp[1][c0 - HX]; s.wyp = wp[1][c0 + HX];
-      s.wymm = wp[1][c0 - 2 * HX]; s.wypp = wp[1][c0 + 2 * HX];
-      s.wzm = wp[0][c0]; s.wzp = wp[2][c0];
-      s.pc = (z == g.NZ - 3) ? 0.f : pc[c0];
-      s.pxm = pc[c0 - 1]; s.pym = pc[c0 - HX]; s.pzm = pzm[c0];
+      s.uc = C.x; s.uxm = XM.x; s.uxp = XP.x; s.uym = YM.x; s.uyp = YP.x;
+      s.uymm = YMM.x; s.uypp = YPP.x; s.uzm = ZM.x; s.uzp = ZP.x; s.uzmm = ZMM.x; s.uzpp = ZPP.x;
+      s.vc = C.y; s.vxm = XM.y; s.vxp = XP.y; s.vxmm = XMM.y; s.vxpp = XPP.y; s.vym = YM.y;
+      s.vyp = YP.y; s.vzm = ZM.y; s.vzp = ZP.y; s.vzmm = ZMM.y; s.vzpp = ZPP.y;
+      s.wc = C.z; s.wxm = XM.z; s.wxp = XP.z; s.wxmm = XMM.z; s.wxpp = XPP.z; s.wym = YM.z;
+      s.wyp = YP.z; s.wymm = YMM.z; s.wypp = YPP.z; s.wzm = ZM.z; s.wzp = ZP.z;
+      s.pc = (z == g.NZ - 3) ? 0.f : C.w;
+      s.pxm = XM.w; s.pym = YM.w; s.pzm = ZM.w;
       float un, vn, wn, pn;
       update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
-      un += rr[0][t];
-      vn += rr[1][t];
-      wn += rr[2][t];
-      pn += rr[3][t];
+      const float4 r = S.r[sr][t];
       const int x = bx * TX + lx + 2, y = by * TY + ly + 2;
-      write_voxel<float, true>(E2, (long long)z * pl + (long long)y * px + x, x, y, z, g, px, pl,
-                               un, vn, wn, pn);
+      write_voxel4(E2, (long long)z * pl + (long long)y * px + x, x, y, z, g, un + r.x,
+                   vn + r.y, wn + r.z, pn + r.w);
     }
     __syncthreads();  // every thread is done with the slots group j+D+1 reuses
     if (leader && issued < L) {
@@ -283,6 +255,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+// 3-D map over a padded array: dims {pitch elements, NY, NZ}.
 bool encode(CUtensorMap* m, CUtensorMapDataType t, int esize, void* base, const Grid& g,
             long long pitch, unsigned bx, unsigned by) {
   auto fn = encode_fn();
@@ -302,7 +275,7 @@ struct ZmarchPlan {
   Maps maps[2];  // source buffer E0 / E1
   int* err = nullptr;
   int zchunk = 0;
-  int tile = 0;  // 0: 32 x 16, 1: 64 x 8
+  int tile = 0;  // 0: 32 x 16, 1: 32 x 8
   dim3 grid;
 };
 
@@ -321,26 +294,23 @@ static void set_smem_attr() {
   done = true;
 }
 
-cudaError_t zmarch_create(ZmarchPlan** out, const Grid& g, Fields<float> E0, Fields<float> E1,
-                          Fields<float> R, const uint8_t* codes, int zchunk, int tile) {
+cudaError_t zmarch_create(ZmarchPlan** out, const Grid& g, float4* E0, float4* E1, float4* R,
+                          const uint8_t* codes, int zchunk, int tile) {
   *out = nullptr;
   ZmarchPlan* pl = new ZmarchPlan();
   pl->tile = tile;
   const int TX = tile ? TileB::TX : TileA::TX, TY = tile ? TileB::TY : TileA::TY;
-  const unsigned HX = TX + 8, HY = TY + 4;
-  Fields<float> src[2] = {E0, E1};
+  const size_t smem = tile ? sizeof(Smem<TileB>) : sizeof(Smem<TileA>);
+  const int per_sm = tile ? 3 : 2;  // resident CTAs per SM at this shared-memory size
+  float4* src[2] = {E0, E1};
   bool ok = true;
   for (int b = 0; b < 2; ++b) {
-    float* f[4] = {src[b].u, src[b].v, src[b].w, src[b].p};
-    float* rf[4] = {R.u, R.v, R.w, R.p};
-    for (int k = 0; k < 4; ++k) {
-      ok &= encode(&pl->maps[b].e[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f[k] - kXoff32, g,
-                   g.px32, HX, HY);
-      ok &= encode(&pl->maps[b].r[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, rf[k] - kXoff32, g,
-                   g.px32, TX, TY);
-    }
-    ok &= encode(&pl->maps[b].codes, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1,
-                 (void*)(codes - kXoffC), g, g.pxc, TX, TY);
+    ok &= encode(&pl->maps[b].e, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src[b] - kXoff4, g,
+                 4LL * g.px4, 4 * (TX + 4), TY + 4);
+    ok &= encode(&pl->maps[b].r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, R - kXoff4, g, 4LL * g.px4,
+                 4 * TX, TY);
+    ok &= encode(&pl->maps[b].codes, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, (void*)(codes - kXoffC),
+                 g, g.pxc, TX, TY);
   }
   if (!ok) {
     delete pl;
@@ -357,12 +327,13 @@ cudaError_t zmarch_create(ZmarchPlan** out, const Grid& g, Fields<float> E0, Fie
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // one wave: at most two resident CTAs per SM, so no partial second wave
-    long long slots = 2LL * sms;
+    // one wave of resident CTAs, never a partial second wave
+    long long slots = (long long)per_sm * sms;
     int nch = (int)std::max(1LL, slots / ((long long)gx * gy));
     zchunk = (g.nz + nch - 1) / nch;
     if (zchunk < 8) zchunk = std::min(8, g.nz);
   }
+  (void)smem;
   pl->zchunk = zchunk;
   pl->grid = dim3(gx, gy, (g.nz + zchunk - 1) / zchunk);
   if (tile) set_smem_attr<TileB>();
@@ -378,7 +349,7 @@ void zmarch_destroy(ZmarchPlan* pl) {
 }
 
 template <class T>
-static void launch_t(const ZmarchPlan* pl, int src, Fields<float> E2, const Grid& g, int solver,
+static void launch_t(const ZmarchPlan* pl, int src, float4* E2, const Grid& g, int solver,
                      cudaStream_t st) {
   const long long budget = 4000000000LL;  // ~2 s at 2 GHz per wait
   const size_t sm = sizeof(Smem<T>);
@@ -393,8 +364,8 @@ static void launch_t(const ZmarchPlan* pl, int src, Fields<float> E2, const Grid
                                                           budget, pl->err);
 }
 
-cudaError_t zmarch_inner(const ZmarchPlan* pl, int src, Fields<float> E2, const Grid& g,
-                         int solver, cudaStream_t st) {
+cudaError_t zmarch_inner(const ZmarchPlan* pl, int src, float4* E2, const Grid& g, int solver,
+                         cudaStream_t st) {
   if (pl->tile) launch_t<TileB>(pl, src, E2, g, solver, st);
   else launch_t<TileA>(pl, src, E2, g, solver, st);
   count_launches(1);

@@ -103,10 +103,10 @@ def footprint(shape):
     NX, NY, NZ = nx + 4, ny + 4, nz + 4
     up = lambda a, b: (a + b - 1) // b * b  # noqa: E731
     a64 = up(14 + NX, 16) * NY * NZ + 64
-    a32 = up(30 + NX, 32) * NY * NZ + 64
+    a4 = up(6 + NX, 8) * NY * NZ + 16
     ac = up(14 + NX, 16) * NY * NZ + 256
     n = nx * ny * nz
-    return ac + 4 * n + 64 * a64 + 48 * a32 + 8 * n + (1 << 20)
+    return ac + 4 * n + 64 * a64 + 48 * a4 + 8 * n + (1 << 20)
 
 
 def test_budget_limits_resident_set_and_all_finish():
