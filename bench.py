@@ -46,9 +46,10 @@ def parse():
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--workload", choices=["c2", "c4", "c5"], default="c2",
-                    help="c2: 128^3 tensor workload (default); c4: batched uneven samples; "
-                         "c5: serving stream with Poisson arrivals")
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
+                    help="c2: 128^3 tensor workload (default); c3: one 512^3 sample "
+                         "(HBM-streaming roofline); c4: batched uneven samples; c5: serving "
+                         "stream with Poisson arrivals")
     ap.add_argument("--samples", type=int, default=64, help="c4/c5: number of requests")
     ap.add_argument("--max-axis", type=int, default=128, help="c5: largest axis length")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
@@ -515,10 +516,65 @@ def run_c5(args):
     return 0
 
 
+def run_c3(args):
+    """One large sample: iid N(0,1) -> periodic Gaussian filter sigma 3 ->
+    fluid = lowest 20 % -> largest z-percolating cluster; boundary_method 2,
+    GS update (solving_algorithm 2); FP64 red-black, FP64 Jacobi and the mixed
+    form timed over it_eval blocks, and the correction sweep's roofline with a
+    working set far above L2."""
+    import poremaps_gb300 as pm
+    from poremaps_gb300 import synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pm.set_device(local)
+    n = args.size if args.size != 128 else 512
+    t0 = time.perf_counter()
+    g = synth.gaussian_field((n, n, n), 3.0, 0.20, seed=3)
+    t_gen = time.perf_counter() - t0
+    kw = dict(boundary_method=2, solving_algorithm=2, voxel_size=5e-6, eps=1e-6, it_eval=100,
+              it_write=100)
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    forms = {}
+    for name, extra in (("mixed", dict(precision="mixed", order="jacobi")),
+                        ("fp64_jacobi", dict(precision="fp64", order="jacobi")),
+                        ("fp64_redblack", dict(precision="fp64", order="redblack"))):
+        with pm.Problem(g, None, **extra, **kw) as p:
+            perm = 0.0
+            for _ in range(max(1, args.warmup)):
+                _, _, perm = p.block_timed(SWEEPS_PER_BLOCK, True, perm)
+            ms = []
+            for _ in range(max(2, args.steps // 2)):
+                t, _, perm = p.block_timed(SWEEPS_PER_BLOCK, True, perm)
+                ms.append(t)
+            kms = p.kernel_time(0, 10)
+            f = {"glups": g.size * SWEEPS_PER_BLOCK / (statistics.mean(ms) * 1e-3) / 1e9,
+                 "ms_per_block": statistics.mean(ms), "sweep_kernel_ms": kms}
+            if name == "mixed":
+                f["kernel"] = p.kernel()
+                f["brick"] = list(p.brick())
+                f["roofline"] = {"bound": "hbm", "achieved": g.size * ALGO_BYTES_MIXED_INNER /
+                                 (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s"}
+                f["roofline"]["frac"] = f["roofline"]["achieved"] / peak
+            else:
+                f["hbm_frac_of_measured"] = g.size * ALGO_BYTES_FP64 / (kms * 1e-3) / 1e9 / peak
+            forms[name] = f
+    out = {"metric": "GLUP/s", "value": forms["mixed"]["glups"], "unit": "GLUP/s", "n_gpus": 1,
+           "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": f"Gaussian field {n}^3 (sigma 3, porosity 0.20, largest "
+                                  "z-percolating cluster), boundary_method 2, GS, it_eval blocks",
+                      "porosity": float(1 - g.mean()), "generation_s": t_gen},
+           "forms": forms}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.profile_case:
         return run_profile_case(args)
+    if args.workload == "c3":
+        return run_c3(args)
     if args.workload == "c4":
         return run_c4(args)
     if args.workload == "c5":

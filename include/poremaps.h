@@ -176,6 +176,9 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms);
 /* The correction-sweep kernel a mixed-precision problem uses (pm_params.kernel
  * values; the autotuned choice when it was created with kernel = -1). */
 pm_status pm_get_kernel(pm_problem* pr, int* kernel);
+/* Brick order of the problem's fluid list (x, y, z extents; 0 0 0 = lexicographic
+ * rows): the autotuner's choice for the mixed form. */
+pm_status pm_get_brick(pm_problem* pr, int brick[3]);
 /* Number of kernels this library has launched in this process. */
 uint64_t pm_kernel_launches(void);
 

@@ -80,7 +80,7 @@ EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
            "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
            "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
-           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_reduce_fields_noalloc",
+           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_get_brick", "pm_reduce_fields_noalloc",
            "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms"]
@@ -125,6 +125,7 @@ def load_library(path: str = LIB_PATH):
         "pm_kernel_time": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double)]),
         "pm_kernel_launches": (C.c_uint64, []),
         "pm_get_kernel": (C.c_int, [vp, P(C.c_int)]),
+        "pm_get_brick": (C.c_int, [vp, P(C.c_int)]),
         "pm_reduce_fields_noalloc": (C.c_int, [P(C.c_int), vp, vp, vp, vp, vp, P(C.c_int), vp,
                                                vp]),
         "pm_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
@@ -268,6 +269,12 @@ class Problem:
         k = C.c_int()
         _check(load_library().pm_get_kernel(self.h, C.byref(k)))
         return k.value
+
+    def brick(self):
+        """Brick order of the fluid list chosen for this problem."""
+        b = (C.c_int * 3)()
+        _check(load_library().pm_get_brick(self.h, b))
+        return tuple(b)
 
     def kernel_time(self, kernel: int = 0, n: int = 20) -> float:
         v = C.c_double()

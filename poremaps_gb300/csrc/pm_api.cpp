@@ -144,17 +144,28 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     }
     return PM_OK;
   };
+  auto order = [&](const int* b) -> pm_status {
+    int* dcount = (int*)pr->dout;
+    CK(launch_fluid_list(pr->codes, pr->g, pr->list, dcount, pr->st, b[0], b[1], b[2]));
+    for (int i = 0; i < 3; ++i) pr->brick[i] = b[i];
+    return PM_OK;
+  };
   if (kernel >= 0) {
     if ((kernel == 0 || kernel == 3) && !tma) kernel = 1;
     return make(kernel);
   }
-  int cands[4] = {1, 2, 0, 3};
-  int nc = tma ? 4 : 2;
+  // candidates: (kernel, brick order of the fluid list)
+  struct Cand { int k, b[3]; };
+  const Cand cands[] = {{2, {0, 0, 0}}, {2, {32, 4, 4}}, {2, {32, 8, 8}}, {2, {64, 8, 4}},
+                        {1, {32, 8, 8}}, {0, {0, 0, 0}}, {3, {0, 0, 0}}};
+  const int nc = tma ? 7 : 5;
   float best = 1e30f;
-  int bestk = 1;
+  int bi = 0;
   for (int i = 0; i < nc; ++i) {
-    pm_status s = make(cands[i]);
-    if (s != PM_OK) return s;
+    pm_status s;
+    if ((s = make(cands[i].k)) != PM_OK) return s;
+    if (cands[i].k == 1 || cands[i].k == 2)
+      if ((s = order(cands[i].b)) != PM_OK) return s;
     for (int w = 0; w < 2; ++w)
       if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
     CK(cudaEventRecord(pr->ev0, pr->st));
@@ -164,10 +175,11 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     if ((s = device_sync(pr, "kernel autotune")) != PM_OK) return s;
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
-    if (ms < best) { best = ms; bestk = cands[i]; }
+    if (ms < best) { best = ms; bi = i; }
   }
-  pm_status s = make(bestk);
+  pm_status s = make(cands[bi].k);
   if (s != PM_OK) return s;
+  if ((s = order(cands[bi].b)) != PM_OK) return s;
   CK(launch_zero4(pr->E[0], pr->g, pr->st));
   CK(launch_zero4(pr->E[1], pr->g, pr->st));
   return device_sync(pr, "kernel autotune");
@@ -645,6 +657,12 @@ uint64_t pm_kernel_launches(void) { return (uint64_t)launches_total(); }
 pm_status pm_get_kernel(pm_problem* pr, int* kernel) {
   if (!pr || !kernel) return set_error(PM_ERR_INVALID, "bad arguments");
   *kernel = pr->kern;
+  return PM_OK;
+}
+
+pm_status pm_get_brick(pm_problem* pr, int brick[3]) {
+  if (!pr || !brick) return set_error(PM_ERR_INVALID, "bad arguments");
+  for (int i = 0; i < 3; ++i) brick[i] = pr->brick[i];
   return PM_OK;
 }
 

@@ -35,6 +35,7 @@ struct pm_problem {
   int coop_blocks = 0;
   pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
+  int brick[3] = {0, 0, 0};      // fluid-list order: bricks (0 = lexicographic rows)
   // state
   int cur = 0;        // FP64 state buffer holding the current iterate
   int ecur = 0;       // FP32 correction buffer holding e

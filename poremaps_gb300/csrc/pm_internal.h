@@ -33,6 +33,9 @@ struct Grid {
   long long pl64, pl32, plc, pl4; // plane strides in elements
   long long alloc64, alloc32, allocc, alloc4; // elements to allocate (including XOFF)
   long long nvox;      // nx*ny*nz
+  // n / nx and n / ny for 0 <= n < 2^31 as (n * m) >> (32 + s) (round-up magic)
+  unsigned long long mnx, mny;
+  int snx, sny;
 };
 
 Grid make_grid(int nx, int ny, int nz, int boundary_method);
@@ -68,8 +71,10 @@ unsigned long long launches_total();
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return the launch error.
 cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st);
+// Fluid list in brick order (bx x by x bz bricks; bx <= 0: whole rows,
+// by/bz <= 0: 1, i.e. lexicographic order).
 cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
-                              cudaStream_t st);
+                              cudaStream_t st, int bx = 0, int by = 0, int bz = 0);
 cudaError_t launch_counts(const uint8_t* codes, const Grid& g, const int di[6],
                           unsigned long long* out4, cudaStream_t st);
 cudaError_t launch_init64(Fields<double> f, const uint8_t* codes, const Grid& g,

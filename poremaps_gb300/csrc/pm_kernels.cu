@@ -4,6 +4,7 @@
 // (which is built for x86-64 without FMA contraction).
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "pm_internal.h"
@@ -38,6 +39,15 @@ Grid make_grid(int nx, int ny, int nz, int bm) {
   g.alloc32 = g.pl32 * g.NZ + 64;
   g.allocc = g.plc * g.NZ + 256;
   g.nvox = (long long)nx * ny * nz;
+  // s = ceil(log2 d), m = ceil(2^(32+s) / d): (n m) >> (32+s) == n / d for all
+  // n < 2^31, since the rounding error n (m - 2^(32+s)/d) / 2^(32+s) < 1/(2d).
+  auto magic = [](unsigned d, unsigned long long& m, int& s) {
+    s = 0;
+    while ((1ULL << s) < d) ++s;
+    m = ((1ULL << (32 + s)) + d - 1) / d;
+  };
+  magic((unsigned)nx, g.mnx, g.snx);
+  magic((unsigned)ny, g.mny, g.sny);
   return g;
 }
 
@@ -102,15 +112,40 @@ cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cuda
   return cudaGetLastError();
 }
 
-// Interior fluid voxels in lexicographic order (x fastest) as linear interior
-// indices; built once, used by the sweep kernels so that warps only carry
-// fluid voxels.  Order: one block per (y, z) row with a ballot scan.
-__global__ void k_row_counts(const uint8_t* codes, Grid g, int* row_count) {
-  int row = blockIdx.x;  // z' * ny + y'
-  int yp = row % g.ny, zp = row / g.ny;
-  const uint8_t* c = codes + ((long long)(zp + 2) * g.NY + (yp + 2)) * g.pxc + 2;
+// Interior fluid voxels as linear interior indices, in brick order: the
+// domain is cut into bricks of BX x BY x BZ voxels (BX = nx, BY = BZ = 1 is
+// plain lexicographic order), bricks are visited lexicographically and the
+// voxels inside a brick in x-fastest order.  A thread block's run of the list
+// then covers a compact brick, so the stencil neighbours of its voxels are
+// mostly in L1.  The list is built from "segments": the x-run of one (y, z)
+// row inside one brick, counted, scanned and filled in order (deterministic).
+struct Bricks {
+  int bx, by, bz;     // brick extents
+  int nbx, nby, nbz;  // bricks per axis
+};
+
+__device__ __forceinline__ void segment(const Grid& g, const Bricks& b, int s, int& x0, int& len,
+                                        int& y, int& z) {
+  const int per_brick = b.by * b.bz;
+  const int brick = s / per_brick, in = s - brick * per_brick;
+  const int ix = brick % b.nbx, r = brick / b.nbx;
+  const int iy = r % b.nby, iz = r / b.nby;
+  const int ly = in % b.by, lz = in / b.by;
+  x0 = ix * b.bx;
+  len = min(b.bx, g.nx - x0);
+  y = iy * b.by + ly;
+  z = iz * b.bz + lz;
+  if (y >= g.ny || z >= g.nz) len = 0;
+}
+
+__global__ void k_seg_counts(const uint8_t* codes, Grid g, Bricks b, int* seg_count) {
+  int x0, len, y, z;
+  segment(g, b, blockIdx.x, x0, len, y, z);
   int cnt = 0;
-  for (int x = threadIdx.x; x < g.nx; x += blockDim.x) cnt += c[x] != 0;
+  if (len > 0) {
+    const uint8_t* c = codes + ((long long)(z + 2) * g.NY + (y + 2)) * g.pxc + 2 + x0;
+    for (int x = threadIdx.x; x < len; x += blockDim.x) cnt += c[x] != 0;
+  }
   __shared__ int s[32];
   for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
@@ -118,41 +153,38 @@ __global__ void k_row_counts(const uint8_t* codes, Grid g, int* row_count) {
   if (threadIdx.x == 0) {
     int t = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
-    row_count[row] = t;
+    seg_count[blockIdx.x] = t;
   }
 }
 
-__global__ void k_row_fill(const uint8_t* codes, Grid g, const int* row_off, int* list) {
-  int row = blockIdx.x;
-  int yp = row % g.ny, zp = row / g.ny;
-  const uint8_t* c = codes + ((long long)(zp + 2) * g.NY + (yp + 2)) * g.pxc + 2;
-  __shared__ int base;
-  if (threadIdx.x == 0) base = row_off[row];
-  __syncthreads();
-  int lane = threadIdx.x & 31;
-  for (int x0 = 0; x0 < g.nx; x0 += 32) {
-    // one warp walks the row in order (deterministic, lexicographic)
-    if (threadIdx.x < 32) {
-      int x = x0 + lane;
-      bool f = x < g.nx && c[x] != 0;
-      unsigned m = __ballot_sync(0xffffffffu, f);
-      if (f) list[base + __popc(m & ((1u << lane) - 1))] = (int)(((long long)zp * g.ny + yp) * g.nx + x);
-      if (lane == 0) base += __popc(m);
-      __syncwarp();
-    }
+__global__ void k_seg_fill(const uint8_t* codes, Grid g, Bricks b, const int* seg_off,
+                           int* list) {
+  int x0, len, y, z;
+  segment(g, b, blockIdx.x, x0, len, y, z);
+  if (len <= 0) return;
+  const uint8_t* c = codes + ((long long)(z + 2) * g.NY + (y + 2)) * g.pxc + 2 + x0;
+  int base = seg_off[blockIdx.x];
+  const int lane = threadIdx.x;  // one warp walks the segment in x order
+  for (int xs = 0; xs < len; xs += 32) {
+    const int x = xs + lane;
+    const bool f = x < len && c[x] != 0;
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (f)
+      list[base + __popc(m & ((1u << lane) - 1))] =
+          (int)(((long long)z * g.ny + y) * g.nx + x0 + x);
+    base += __popc(m);
   }
 }
 
 __global__ void k_scan_rows(const int* row_count, int nrows, int* row_off, int* total) {
   // single block, sequential chunks (set-up only)
   __shared__ int carry;
+  __shared__ int s[1024];
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   for (int b = 0; b < nrows; b += blockDim.x) {
     int i = b + threadIdx.x;
     int v = i < nrows ? row_count[i] : 0;
-    // block inclusive scan
-    __shared__ int s[1024];
     s[threadIdx.x] = v;
     __syncthreads();
     for (int o = 1; o < (int)blockDim.x; o <<= 1) {
@@ -170,14 +202,22 @@ __global__ void k_scan_rows(const int* row_count, int nrows, int* row_off, int* 
 }
 
 cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
-                              cudaStream_t st) {
-  int nrows = g.ny * g.nz;
+                              cudaStream_t st, int bx, int by, int bz) {
+  Bricks b;
+  b.bx = bx > 0 ? std::min(bx, g.nx) : g.nx;
+  b.by = by > 0 ? std::min(by, g.ny) : 1;
+  b.bz = bz > 0 ? std::min(bz, g.nz) : 1;
+  b.nbx = (g.nx + b.bx - 1) / b.bx;
+  b.nby = (g.ny + b.by - 1) / b.by;
+  b.nbz = (g.nz + b.bz - 1) / b.bz;
+  const long long nseg = (long long)b.nbx * b.nby * b.nbz * b.by * b.bz;
+  if (nseg > (1LL << 30)) return cudaErrorInvalidValue;
   int* tmp = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&tmp, sizeof(int) * 2 * (size_t)nrows, st);
+  cudaError_t e = cudaMallocAsync((void**)&tmp, sizeof(int) * 2 * (size_t)nseg, st);
   if (e != cudaSuccess) return e;
-  k_row_counts<<<nrows, 128, 0, st>>>(codes, g, tmp);
-  k_scan_rows<<<1, 1024, 0, st>>>(tmp, nrows, tmp + nrows, count);
-  k_row_fill<<<nrows, 32, 0, st>>>(codes, g, tmp + nrows, list);
+  k_seg_counts<<<(unsigned)nseg, 128, 0, st>>>(codes, g, b, tmp);
+  k_scan_rows<<<1, 1024, 0, st>>>(tmp, (int)nseg, tmp + nseg, count);
+  k_seg_fill<<<(unsigned)nseg, 32, 0, st>>>(codes, g, b, tmp + nseg, list);
   count_launches(3);
   e = cudaGetLastError();
   cudaFreeAsync(tmp, st);

@@ -259,12 +259,16 @@ __device__ __forceinline__ void write_voxel(const Fields<T>& B, long long c, int
 // so a sample computes exactly the same values alone and in a batch.
 
 // Interior linear index (x fastest) -> padded coordinates.
+__device__ __forceinline__ unsigned div_magic(unsigned n, unsigned long long m, int s) {
+  return (unsigned)(((unsigned long long)n * m) >> (32 + s));
+}
+
 __device__ __forceinline__ void lin_to_xyz(int lin, const Grid& g, int& x, int& y, int& z) {
-  int xp = lin % g.nx;
-  int r = lin / g.nx;
-  x = xp + 2;
-  y = r % g.ny + 2;
-  z = r / g.ny + 2;
+  const unsigned r = div_magic((unsigned)lin, g.mnx, g.snx);  // lin / nx
+  const unsigned zz = div_magic(r, g.mny, g.sny);             // r / ny
+  x = lin - (int)r * g.nx + 2;
+  y = (int)r - (int)zz * g.ny + 2;
+  z = (int)zz + 2;
 }
 
 // One voxel of an FP64 sweep (Jacobi phase 0, red 1, black 2) from A into B.

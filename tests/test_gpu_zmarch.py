@@ -36,3 +36,18 @@ def test_autotuned_kernel_is_a_candidate():
     g = synth.random_solid((32, 32, 32), 0.3, 1)
     with pm.Problem(g, None, solving_algorithm=2, order="jacobi", precision="mixed") as p:
         assert p.kernel() in (0, 1, 2, 3)
+
+
+@pytest.mark.parametrize("shape,bc", [((40, 36, 70), 0), ((33, 21, 50), 2)])
+def test_autotuned_kernel_and_list_order_bitwise(shape, bc):
+    """Whatever kernel and fluid-list brick order the autotuner picks, the
+    fields equal the lexicographic fluid-list sweep bit for bit."""
+    g = synth.random_solid(shape, 0.3, 5)
+    out = []
+    for kernel in (-1, 1):
+        with pm.Problem(g, None, boundary_method=bc, solving_algorithm=2, order="jacobi",
+                        precision="mixed", kernel=kernel) as p:
+            p.iterate(150)
+            out.append(p.fields())
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
