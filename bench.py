@@ -52,6 +52,10 @@ def parse():
                          "stream with Poisson arrivals")
     ap.add_argument("--samples", type=int, default=64, help="c4/c5: number of requests")
     ap.add_argument("--max-axis", type=int, default=128, help="c5: largest axis length")
+    ap.add_argument("--kernel", type=int, default=-1,
+                    help="profile case: correction-sweep kernel (-1 autotune)")
+    ap.add_argument("--brick", type=int, nargs=3, default=[0, 0, 0],
+                    help="profile case: fluid-list brick order for kernels 1/2")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                     help="run two it_eval blocks of one resident problem and exit (a small, "
                          "self-contained case for ncu captures)")
@@ -212,29 +216,21 @@ def run_reference(args):
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args):
     import torch
-    import torch.distributed as dist
 
     import poremaps_gb300 as pm
+    from poremaps_gb300.replicas import Replicas
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     pm.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    rep = Replicas("nccl")
+    world, rank = rep.world, rep.rank
 
     def barrier():
-        if world > 1:
-            dist.barrier()
+        rep.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    max_over_ranks = rep.max
 
     g, rots = workload(args.size)
     nvox = g.size
@@ -269,34 +265,40 @@ def run_gpu(args):
     lups_step = 3 * SWEEPS_PER_BLOCK * nvox
     value = world * lups_step / (ms_mx * 1e-3) / 1e9
     kernel_ms = probs_mx[2].kernel_time(0, 50)
-    kname = {0: "k_zmarch_inner 32x16 (TMA z-march FP32 correction sweep)",
-             3: "k_zmarch_inner 64x8 (TMA z-march FP32 correction sweep)",
-             1: "k_dc_inner (fluid-list FP32 correction sweep)",
-             2: "k_dc_inner_occ (fluid-list FP32 correction sweep, 4 blocks/SM)"}[
-        probs_mx[2].kernel()]
+    kid = probs_mx[2].kernel()
+    kshort, kdesc = KERNELS[kid]
+    kname = f"{kshort} ({kdesc})"
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = nvox * ALGO_BYTES_MIXED_INNER / (kernel_ms * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_zmarch_inner_sphere128_traffic.json")
+    # DRAM bytes of one launch of the chosen kernel on this workload, from an
+    # ncu capture of `bench.py --profile-case mixed` (profiles/*_traffic.json)
+    tpath = os.path.join(ROOT, "profiles", f"{kshort}_sphere{args.size}_traffic.json")
     if os.path.exists(tpath):
         t = json.load(open(tpath))
         traffic = t["dram_bytes_per_launch"] * nvox / t["nvox"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "kernel": kname, "kernel_choice": "autotuned at problem creation",
+                "brick": list(probs_mx[2].brick()),
+                "kernels_per_rotation": [[KERNELS[p.kernel()][0], list(p.brick())]
+                                         for p in probs_mx],
                 "algorithmic_bytes_per_lup": ALGO_BYTES_MIXED_INNER,
                 "kernel_ms": kernel_ms,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst, of measured)" if peaks
                                else "fallback 6.8 TB/s (of fallback)"}
-    forms = {"mixed": {"glups": value, "ms_per_step": ms_mx, "inner_kernel_ms": kernel_ms}}
+    phi = float(1 - g.mean())  # every rotation has the same fluid count
+    forms = {"mixed": {"glups": value, "fluid_glups": value * phi, "ms_per_step": ms_mx,
+                       "inner_kernel_ms": kernel_ms}}
 
     k_rel = None
     if not args.no_fp64:
         probs_64, perm_64, ms_64, _, _ = timed_form("fp64", max(2, args.steps // 2),
                                                     max(1, args.warmup))
         k64 = probs_64[2].kernel_time(0, 10)
-        forms["fp64"] = {"glups": world * lups_step / (ms_64 * 1e-3) / 1e9, "ms_per_step": ms_64,
+        glups64 = world * lups_step / (ms_64 * 1e-3) / 1e9
+        forms["fp64"] = {"glups": glups64, "fluid_glups": glups64 * phi, "ms_per_step": ms_64,
                          "sweep_kernel_ms": k64,
                          "hbm_frac_of_measured": nvox * ALGO_BYTES_FP64 / (k64 * 1e-3) / 1e9 / peak,
                          "note": "FP64 sweeps are bound by the FP64 pipe of GB300, not by HBM"}
@@ -357,19 +359,27 @@ def run_gpu(args):
         if k_rel is not None:
             out["k_rel_diff_vs_fp64"] = k_rel
         print(json.dumps(out), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    rep.close()
     return 0
+
+
+KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep"),
+           3: ("k_zmarch_inner", "32x8 tiles, TMA z-march FP32 correction sweep"),
+           1: ("k_dc_inner", "fluid-list FP32 correction sweep"),
+           2: ("k_dc_inner_occ", "fluid-list FP32 correction sweep, 4 blocks/SM")}
 
 
 def run_profile_case(args):
     import poremaps_gb300 as pm
 
     g, rots = workload(args.size)
-    with pm.Problem(rots[0], None, precision=args.profile_case, solving_algorithm=3,
-                    boundary_method=0, voxel_size=1e-5, order="jacobi") as p:
+    with pm.Problem(rots[2], None, precision=args.profile_case, solving_algorithm=3,
+                    boundary_method=0, voxel_size=1e-5, order="jacobi", kernel=args.kernel,
+                    brick=args.brick) as p:
         for _ in range(2):
             p.block_timed(SWEEPS_PER_BLOCK, True)
+        if args.profile_case == "mixed":
+            print(json.dumps({"kernel": KERNELS[p.kernel()][0], "brick": p.brick()}), flush=True)
     return 0
 
 

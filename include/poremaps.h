@@ -100,6 +100,8 @@ typedef struct {
                                    the fastest), 0 TMA z-march 32x16 tiles, 3 TMA
                                    z-march 64x8 tiles, 1 fluid-list gather, 2 fluid-list
                                    gather at four blocks per SM */
+  int brick[3];                 /* fluid-list order of kernels 1/2 when kernel >= 0:
+                                   brick extents x y z (voxels), 0 0 0 = lexicographic */
 } pm_params;
 
 typedef struct {
@@ -142,6 +144,18 @@ pm_status pm_get_iteration(pm_problem* pr, int* iteration);
 /* Interior fields, x fastest, nx*ny*nz doubles each; any pointer may be NULL.
  * Unscaled (the writers multiply velocities by voxel_size). */
 pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double* p);
+/* Restart from interior fields (the inverse of pm_get_fields): replaces the
+ * state, refreshes the periodic halos, reapplies the pressure planes and sets
+ * the iteration counter.  The next convergence check compares against k = 0,
+ * as the first check of a fresh run does.  No counterpart in the reference
+ * (it has no restart); it is the resume half of checkpointing through the
+ * field dumps. */
+pm_status pm_set_fields(pm_problem* pr, const double* u, const double* v, const double* w,
+                        const double* p, int iteration);
+/* Reads velx_/vely_/velz_/press_<geometry_file_name> from the working
+ * directory as pm_write_outputs wrote them (velocities divided by voxel_size)
+ * and calls pm_set_fields.  No counterpart in the reference. */
+pm_status pm_resume_outputs(pm_problem* pr, int iteration);
 /* Interior neighbourhood codes 100*cx + 10*cy + cz (-1 solid), x fastest. */
 pm_status pm_get_neighborhood(pm_problem* pr, int32_t* out);
 /* Writes velx_/vely_/velz_/press_/voxel_neighborhood_/domain_decomp_ + geometry name per

@@ -49,7 +49,8 @@ class Params(C.Structure):
                 ("solving_algorithm", C.c_uint), ("eps", C.c_double), ("porosity", C.c_double),
                 ("dom_interest", C.c_int * 6), ("write_output", C.c_int * 4),
                 ("order", C.c_int), ("precision", C.c_int), ("arith", C.c_int),
-                ("write_log", C.c_int), ("mixed_inner", C.c_int), ("kernel", C.c_int)]
+                ("write_log", C.c_int), ("mixed_inner", C.c_int), ("kernel", C.c_int),
+                ("brick", C.c_int * 3)]
 
 
 class Result(C.Structure):
@@ -78,7 +79,8 @@ class Completion(C.Structure):
 EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_read_geometry", "pm_problem_create", "pm_problem_destroy", "pm_solve",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
-           "pm_get_iteration", "pm_get_fields", "pm_get_neighborhood", "pm_write_outputs",
+           "pm_get_iteration", "pm_get_fields", "pm_set_fields", "pm_resume_outputs",
+           "pm_get_neighborhood", "pm_write_outputs",
            "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
            "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_get_brick", "pm_reduce_fields_noalloc",
            "pm_server_create", "pm_server_destroy",
@@ -114,6 +116,8 @@ def load_library(path: str = LIB_PATH):
         "pm_get_porosity": (C.c_int, [vp, P(C.c_double)]),
         "pm_get_iteration": (C.c_int, [vp, P(C.c_int)]),
         "pm_get_fields": (C.c_int, [vp, vp, vp, vp, vp]),
+        "pm_set_fields": (C.c_int, [vp, vp, vp, vp, vp, C.c_int]),
+        "pm_resume_outputs": (C.c_int, [vp, C.c_int]),
         "pm_get_neighborhood": (C.c_int, [vp, vp]),
         "pm_write_outputs": (C.c_int, [vp]),
         "pm_run_inp": (C.c_int, [C.c_char_p, P(Params), P(Result)]),
@@ -162,7 +166,7 @@ def default_params(**kw) -> Params:
             v = ARITHS[v]
         if k in ("geometry_file_name", "log_file_name"):
             v = v.encode() if isinstance(v, str) else v
-        if k in ("size", "dom_interest", "write_output", "dom_decomposition"):
+        if k in ("size", "dom_interest", "write_output", "dom_decomposition", "brick"):
             arr = getattr(p, k)
             for i, x in enumerate(v):
                 arr[i] = x
@@ -243,6 +247,24 @@ class Problem:
         arr = [np.empty(self.shape, np.float64) for _ in range(4)]
         _check(load_library().pm_get_fields(self.h, *[a.ctypes.data for a in arr]))
         return arr  # u, v, w, p
+
+    @property
+    def iteration(self) -> int:
+        v = C.c_int()
+        _check(load_library().pm_get_iteration(self.h, C.byref(v)))
+        return v.value
+
+    def set_fields(self, u, v, w, p, iteration: int = 0) -> None:
+        """Restart from interior fields (lattice units, as fields() returns)."""
+        arr = [np.ascontiguousarray(a, np.float64) for a in (u, v, w, p)]
+        for a in arr:
+            if a.shape != self.shape:
+                raise ValueError(f"field shape {a.shape} != {self.shape}")
+        _check(load_library().pm_set_fields(self.h, *[a.ctypes.data for a in arr], int(iteration)))
+
+    def resume_outputs(self, iteration: int) -> None:
+        """Restart from the field files write_outputs() left in the working directory."""
+        _check(load_library().pm_resume_outputs(self.h, int(iteration)))
 
     def nhood(self) -> np.ndarray:
         out = np.empty(self.shape, np.int32)

@@ -76,6 +76,13 @@ pm_status validate(const pm_params* p) {
   if (p->order < -1 || p->order > 2) return set_error(PM_ERR_INVALID, "bad order %d", p->order);
   if (p->precision < 0 || p->precision > 1)
     return set_error(PM_ERR_INVALID, "bad precision %d", p->precision);
+  {
+    const int* b = p->brick;
+    const bool none = !b[0] && !b[1] && !b[2], all = b[0] > 0 && b[1] > 0 && b[2] > 0;
+    if (!none && !all)
+      return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
+  }
+  if (p->kernel < -1 || p->kernel > 3) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
     return set_error(PM_ERR_INVALID,
                      "mixed precision sweeps in Jacobi order, which diverges for solver 1 "
@@ -152,7 +159,12 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   };
   if (kernel >= 0) {
     if ((kernel == 0 || kernel == 3) && !tma) kernel = 1;
-    return make(kernel);
+    pm_status s = make(kernel);
+    if (s != PM_OK) return s;
+    const int* b = pr->prm.brick;
+    if ((kernel == 1 || kernel == 2) && (b[0] || b[1] || b[2]) && (s = order(b)) != PM_OK)
+      return s;
+    return device_sync(pr, "kernel choice");
   }
   // candidates: (kernel, brick order of the fluid list)
   struct Cand { int k, b[3]; };
@@ -682,6 +694,32 @@ pm_status pm_get_fields(pm_problem* pr, double* u, double* v, double* w, double*
     if ((s = device_sync(pr, "pm_get_fields")) != PM_OK) return s;
   }
   return PM_OK;
+}
+
+pm_status pm_set_fields(pm_problem* pr, const double* u, const double* v, const double* w,
+                        const double* p, int iteration) {
+  if (!pr || !u || !v || !w || !p || iteration < 0)
+    return set_error(PM_ERR_INVALID, "bad arguments");
+  pm_status s;
+  if ((s = reset_state(pr)) != PM_OK) return s;
+  // The state is a function of the interior: periodic halos are copies and
+  // the pressure planes are reapplied.  The pre-reapply pressure of the last
+  // interior plane is not in the dumps; the reapplied value stands in for it.
+  const Fields<double>& f = pr->F[0];
+  double* dst[4] = {f.u, f.v, f.w, f.p};
+  const double* src[4] = {u, v, w, p};
+  for (int k = 0; k < 4; ++k) {
+    CK(cudaMemcpyAsync(pr->scratch, src[k], sizeof(double) * pr->g.nvox, cudaMemcpyHostToDevice,
+                       pr->st));
+    CK(launch_unpack64((const double*)pr->scratch, pr->g, dst[k], pr->st));
+    // the staging buffer is reused: finish this field before the next copy
+    if ((s = device_sync(pr, "pm_set_fields")) != PM_OK) return s;
+  }
+  CK(launch_halo64(f, pr->g, pr->st));
+  CK(launch_reapply64(f.p, pr->codes, pr->g, pr->st));
+  CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
+  pr->iteration = iteration;
+  return device_sync(pr, "pm_set_fields");
 }
 
 pm_status pm_get_neighborhood(pm_problem* pr, int32_t* out) {

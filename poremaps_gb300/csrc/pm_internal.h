@@ -124,6 +124,7 @@ cudaError_t launch_reduce_serial(Fields<double> x, int full, const uint8_t* code
 
 cudaError_t launch_pack64(const double* f, const uint8_t* codes, int implied3, const Grid& g,
                           double* out, cudaStream_t st);
+cudaError_t launch_unpack64(const double* in, const Grid& g, double* f, cudaStream_t st);
 cudaError_t launch_pack_codes(const uint8_t* codes, const Grid& g, int* out, cudaStream_t st);
 
 

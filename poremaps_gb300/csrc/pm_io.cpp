@@ -129,6 +129,29 @@ pm_status pm_write_outputs(pm_problem* pr) {
   return PM_OK;
 }
 
+pm_status pm_resume_outputs(pm_problem* pr, int iteration) {
+  if (!pr) return set_error(PM_ERR_INVALID, "bad arguments");
+  const pm_params* p = problem_params(pr);
+  const long long n = problem_nvox(pr);
+  const std::string g = p->geometry_file_name;
+  const char* pre[4] = {"velx_", "vely_", "velz_", "press_"};
+  std::vector<double> f[4];
+  for (int k = 0; k < 4; ++k) {
+    f[k].resize((size_t)n);
+    const std::string name = pre[k] + g;
+    FILE* fp = fopen(name.c_str(), "rb");
+    if (!fp) return set_error(PM_ERR_IO, "cannot open %s", name.c_str());
+    size_t got = fread(f[k].data(), sizeof(double), (size_t)n, fp);
+    fclose(fp);
+    if (got != (size_t)n) return set_error(PM_ERR_IO, "%s: short file", name.c_str());
+  }
+  // the writers store velocities times voxel_size
+  const double dx = p->voxel_size;
+  for (int k = 0; k < 3; ++k)
+    for (long long i = 0; i < n; ++i) f[k][i] /= dx;
+  return pm_set_fields(pr, f[0].data(), f[1].data(), f[2].data(), f[3].data(), iteration);
+}
+
 pm_status pm_run_inp(const char* inp_path, const pm_params* overrides, pm_result* res) {
   pm_params p;
   pm_status s = pm_read_params(inp_path, &p);

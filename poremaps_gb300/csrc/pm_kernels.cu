@@ -689,6 +689,23 @@ cudaError_t launch_pack64(const double* f, const uint8_t* codes, int implied3, c
   return cudaGetLastError();
 }
 
+// Inverse of k_pack64: interior values (x fastest) into the padded field.
+__global__ void k_unpack64(const double* in, Grid g, double* f) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;
+       q += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(q % g.nx);
+    long long r = q / g.nx;
+    int y = (int)(r % g.ny), z = (int)(r / g.ny);
+    f[(long long)(z + 2) * g.pl64 + (long long)(y + 2) * g.px64 + x + 2] = in[q];
+  }
+}
+
+cudaError_t launch_unpack64(const double* in, const Grid& g, double* f, cudaStream_t st) {
+  k_unpack64<<<1184, 256, 0, st>>>(in, g, f);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // Neighbourhood codes as the reference stores them: 100cx + 10cy + cz, -1 solid.
 __global__ void k_pack_codes(const uint8_t* codes, Grid g, int* out) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.nvox;

@@ -34,7 +34,19 @@ def channel(nx=24, ny=14, nz=50, frame=2):
     return g
 
 
+def rotate(g, rot):
+    """Axis rotation of README.md:221-225: flow along x (z' = x, y' = z,
+    x' = y) or along y (z' = y, y' = x, x' = z); the array is (z, y, x)."""
+    if rot == "x":
+        return np.ascontiguousarray(np.transpose(g, (2, 0, 1)))
+    if rot == "y":
+        return np.ascontiguousarray(np.transpose(g, (1, 2, 0)))
+    return g
+
+
 def geometry(spec):
+    if "rot" in spec:
+        return rotate(geometry({k: v for k, v in spec.items() if k != "rot"}), spec["rot"])
     kind = spec["kind"]
     if kind == "random":
         return synth.random_solid(tuple(spec["shape"]), spec["frac"], spec["seed"])
@@ -91,6 +103,11 @@ CASES = [
     dict(name="channel_24_14_50", geom={"kind": "channel", "size": [24, 14, 50]}, bc=0, solver=2,
          max_iter=100000001, eps=1e-7, fields=False, porosity=1.0, dx=5e-5),
 ]
+TENSOR_GEOM = {"kind": "spheres", "shape": [16, 16, 16], "rmin": 1.5, "rmax": 3.0, "solid": 0.55,
+               "seed": 11}
+TENSOR = [dict(name=f"tensor_s{solver}_{rot}", geom=dict(TENSOR_GEOM, rot=rot), bc=0,
+               solver=solver, max_iter=400000, eps=1e-10 if solver == 3 else 1e-9, fields=False)
+          for solver in (1, 2, 3) for rot in ("x", "y", "z")]
 SLOW = [
     dict(name="c1_cylinder", geom={"kind": "cylinder", "size": [48, 48, 64], "radius": 20.0},
          bc=0, solver=2, max_iter=100000001, eps=1e-6, fields=False, dx=2e-5),
@@ -131,7 +148,9 @@ def run_case(c):
 
 
 def main():
-    cases = CASES + (SLOW if "--slow" in sys.argv else [])
+    cases = CASES + TENSOR + (SLOW if "--slow" in sys.argv else [])
+    if "--only-tensor" in sys.argv:
+        cases = TENSOR
     path = os.path.join(HERE, "golden.npz")
     old = dict(np.load(path, allow_pickle=False)) if os.path.exists(path) else {}
     store = dict(old)
