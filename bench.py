@@ -281,7 +281,7 @@ def run_gpu(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "kernel": kname, "kernel_choice": "autotuned at problem creation",
-                "brick": list(probs_mx[2].brick()),
+                "kernel_id": kid, "brick": list(probs_mx[2].brick()),
                 "kernels_per_rotation": [[KERNELS[p.kernel()][0], list(p.brick())]
                                          for p in probs_mx],
                 "algorithmic_bytes_per_lup": ALGO_BYTES_MIXED_INNER,
@@ -366,7 +366,10 @@ def run_gpu(args):
 KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep"),
            3: ("k_zmarch_inner", "32x8 tiles, TMA z-march FP32 correction sweep"),
            1: ("k_dc_inner", "fluid-list FP32 correction sweep"),
-           2: ("k_dc_inner_occ", "fluid-list FP32 correction sweep, 4 blocks/SM")}
+           2: ("k_dc_inner_occ", "fluid-list FP32 correction sweep, 4 blocks/SM"),
+           4: ("k_brick_inner", "TMA brick tiles, FP32 correction sweep"),
+           5: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 4 blocks/SM"),
+           6: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 5 blocks/SM")}
 
 
 def run_profile_case(args):

@@ -96,12 +96,17 @@ typedef struct {
   int write_log;                /* 1: append the reference log rows to log_file_name */
   int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
   int kernel;                   /* correction sweep of the mixed form: -1 autotune
-                                   (default: time every candidate on the problem, keep
-                                   the fastest), 0 TMA z-march 32x16 tiles, 3 TMA
-                                   z-march 64x8 tiles, 1 fluid-list gather, 2 fluid-list
-                                   gather at four blocks per SM */
-  int brick[3];                 /* fluid-list order of kernels 1/2 when kernel >= 0:
-                                   brick extents x y z (voxels), 0 0 0 = lexicographic */
+                                   (default: time the fluid-list kernels 5, 2, 1 in a
+                                   few list orders on the problem, keep the fastest),
+                                   0 TMA z-march 32x16 tiles, 3 TMA
+                                   z-march 32x8 tiles, 1 fluid-list gather, 2 fluid-list
+                                   gather at four blocks per SM, 4 TMA bricks (one
+                                   brick + halo per CTA in shared memory), 5 / 6
+                                   persistent fluid-list gather, list prefetched, at
+                                   four / five blocks per SM */
+  int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
+                                   x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
+                                   32 8 8 (default), 32 8 4 or 32 4 4 */
 } pm_params;
 
 typedef struct {

@@ -30,6 +30,7 @@ UNITS = [
     ("pm_kernels.cu", ["-fmad=false"]),
     ("pm_fast.cu", []),
     ("pm_zmarch.cu", []),
+    ("pm_brick.cu", []),
     ("pm_api.cpp", []),
     ("pm_io.cpp", []),
     ("pm_server.cpp", []),

@@ -82,7 +82,9 @@ pm_status validate(const pm_params* p) {
     if (!none && !all)
       return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
   }
-  if (p->kernel < -1 || p->kernel > 3) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel < -1 || p->kernel > 6) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel == 4 && p->brick[0] && pm::brick_shape_of(p->brick[0], p->brick[1], p->brick[2]) < 0)
+    return set_error(PM_ERR_INVALID, "kernel 4 bricks are 32x8x8, 32x8x4 or 32x4x4");
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
     return set_error(PM_ERR_INVALID,
                      "mixed precision sweeps in Jacobi order, which diverges for solver 1 "
@@ -93,14 +95,16 @@ pm_status validate(const pm_params* p) {
 pm_status device_sync(pm_problem* pr, const char* where) {
   cudaError_t e = cudaStreamSynchronize(pr->st);
   if (e != cudaSuccess) return cuda_error(e, where);
-  if (pr->zp) {
+  int* flags[2] = {pr->zp ? zmarch_error_flag(pr->zp) : nullptr,
+                   pr->bp ? brick_error_flag(pr->bp) : nullptr};
+  for (int* f : flags) {
+    if (!f) continue;
     int flag = 0;
-    e = cudaMemcpy(&flag, zmarch_error_flag(pr->zp), sizeof(int), cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(&flag, f, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_error(e, where);
     if (flag) {
-      cudaMemset(zmarch_error_flag(pr->zp), 0, sizeof(int));
-      return set_error(PM_ERR_CUDA, "%s: a TMA pipeline wait of the z-march sweep timed out",
-                       where);
+      cudaMemset(f, 0, sizeof(int));
+      return set_error(PM_ERR_CUDA, "%s: a TMA wait of the correction sweep timed out", where);
     }
   }
   return PM_OK;
@@ -110,6 +114,11 @@ pm_status device_sync(pm_problem* pr, const char* where) {
 pm_status correction_sweep(pm_problem* pr, int src) {
   if (pr->zp) {
     CK(zmarch_inner(pr->zp, src, pr->E[1 - src], pr->g, pr->solver, pr->st));
+  } else if (pr->bp) {
+    CK(brick_inner(pr->bp, src, pr->E[1 - src], pr->R, pr->list, pr->g, pr->solver, pr->st));
+  } else if (pr->kern == 5 || pr->kern == 6) {
+    CK(launch_dc_inner_pf(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist,
+                          pr->g, pr->solver, pr->kern == 6 ? 5 : 4, pr->st));
   } else if (pr->kern == 2) {
     CK(launch_dc_inner_occ(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist,
                            pr->g, pr->solver, pr->st));
@@ -137,61 +146,77 @@ pm_status iterate64(pm_problem* pr) {
 }
 
 // Correction-sweep kernels of the mixed form: 0 TMA z-march with 32 x 16
-// tiles, 3 the same with 64 x 8 tiles, 1 fluid-list gather, 2 fluid-list
-// gather compiled for four blocks per SM.  kernel < 0 times every candidate
-// on this problem (a few launches each; the correction buffers are scratch
-// until the first residual sweep) and keeps the fastest.
+// tiles, 3 the same with 32 x 8 tiles, 1 fluid-list gather, 2 fluid-list
+// gather compiled for four blocks per SM, 4 TMA bricks (32x8x8, 32x8x4 or
+// 32x4x4 voxels per CTA, the fluid list in the same brick order), 5 and 6
+// persistent fluid-list gather with the list prefetched (4 / 5 CTAs per SM).
+// kernel < 0 times the fluid-list candidates on this problem (a few launches
+// each; the correction buffers are scratch until the first residual sweep)
+// and keeps the fastest.
 pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   const bool tma = zmarch_available() != 0;
-  auto make = [&](int k) -> pm_status {
+  // set up kernel k with the fluid list in brick order b (k 1, 2, 4)
+  auto make = [&](int k, const int* b) -> pm_status {
     if (pr->zp) { zmarch_destroy(pr->zp); pr->zp = nullptr; }
+    if (pr->bp) { brick_destroy(pr->bp); pr->bp = nullptr; }
     pr->kern = k;
-    if (k == 0 || k == 3) {
-      CK(zmarch_create(&pr->zp, pr->g, pr->E[0], pr->E[1], pr->R, pr->codes, 0, k == 3));
+    {
+      int* dcount = (int*)pr->dout;
+      CK(launch_fluid_list(pr->codes, pr->g, pr->list, dcount, pr->st, b[0], b[1], b[2]));
+      for (int i = 0; i < 3; ++i) pr->brick[i] = b[i];
     }
+    if (k == 0 || k == 3)
+      CK(zmarch_create(&pr->zp, pr->g, pr->E[0], pr->E[1], pr->R, pr->codes, 0, k == 3));
+    if (k == 4)
+      CK(brick_create(&pr->bp, pr->g, pr->E[0], pr->E[1], pr->codes, pr->list, pr->nlist,
+                      brick_shape_of(b[0], b[1], b[2]), pr->st));
     return PM_OK;
   };
-  auto order = [&](const int* b) -> pm_status {
-    int* dcount = (int*)pr->dout;
-    CK(launch_fluid_list(pr->codes, pr->g, pr->list, dcount, pr->st, b[0], b[1], b[2]));
-    for (int i = 0; i < 3; ++i) pr->brick[i] = b[i];
-    return PM_OK;
-  };
+  static const int kLex[3] = {0, 0, 0};
   if (kernel >= 0) {
-    if ((kernel == 0 || kernel == 3) && !tma) kernel = 1;
-    pm_status s = make(kernel);
-    if (s != PM_OK) return s;
+    if ((kernel == 0 || kernel == 3 || kernel == 4) && !tma) kernel = 1;
     const int* b = pr->prm.brick;
-    if ((kernel == 1 || kernel == 2) && (b[0] || b[1] || b[2]) && (s = order(b)) != PM_OK)
-      return s;
+    static const int kBrick0[3] = {32, 8, 8};
+    if (kernel == 4 && !b[0]) b = kBrick0;
+    pm_status s = make(kernel, (kernel == 0 || kernel == 3) ? kLex : b);
+    if (s != PM_OK) return s;
     return device_sync(pr, "kernel choice");
   }
   // candidates: (kernel, brick order of the fluid list)
   struct Cand { int k, b[3]; };
-  const Cand cands[] = {{2, {0, 0, 0}}, {2, {32, 4, 4}}, {2, {32, 8, 8}}, {2, {64, 8, 4}},
-                        {1, {32, 8, 8}}, {0, {0, 0, 0}}, {3, {0, 0, 0}}};
-  const int nc = tma ? 7 : 5;
-  float best = 1e30f;
-  int bi = 0;
+  // The TMA kernels (0, 3, 4) and kernel 6 lose on every medium measured so
+  // far and are left to explicit choice; timing them would only lengthen the
+  // set-up of every problem.
+  const Cand cands[] = {{5, {0, 0, 0}}, {5, {32, 8, 8}}, {5, {32, 4, 4}}, {2, {0, 0, 0}},
+                        {1, {32, 8, 8}}};
+  const int nc = 5;
+  // Each candidate: the best of three timings of five sweeps.  The first
+  // candidate is kept unless another one is at least 2 % faster, so timing
+  // noise does not flip the choice between near-equal kernels.
+  float t[5];
   for (int i = 0; i < nc; ++i) {
     pm_status s;
-    if ((s = make(cands[i].k)) != PM_OK) return s;
-    if (cands[i].k == 1 || cands[i].k == 2)
-      if ((s = order(cands[i].b)) != PM_OK) return s;
+    if ((s = make(cands[i].k, cands[i].b)) != PM_OK) return s;
     for (int w = 0; w < 2; ++w)
       if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
-    CK(cudaEventRecord(pr->ev0, pr->st));
-    for (int r = 0; r < 5; ++r)
-      if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
-    CK(cudaEventRecord(pr->ev1, pr->st));
-    if ((s = device_sync(pr, "kernel autotune")) != PM_OK) return s;
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
-    if (ms < best) { best = ms; bi = i; }
+    t[i] = 1e30f;
+    for (int trial = 0; trial < 3; ++trial) {
+      CK(cudaEventRecord(pr->ev0, pr->st));
+      for (int r = 0; r < 5; ++r)
+        if ((s = correction_sweep(pr, 0)) != PM_OK) return s;
+      CK(cudaEventRecord(pr->ev1, pr->st));
+      if ((s = device_sync(pr, "kernel autotune")) != PM_OK) return s;
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+      if (ms < t[i]) t[i] = ms;
+    }
   }
-  pm_status s = make(cands[bi].k);
+  int bi = 0;
+  for (int i = 1; i < nc; ++i)
+    if (t[i] < t[bi]) bi = i;
+  if (t[bi] > 0.98f * t[0]) bi = 0;
+  pm_status s = make(cands[bi].k, cands[bi].b);
   if (s != PM_OK) return s;
-  if ((s = order(cands[bi].b)) != PM_OK) return s;
   CK(launch_zero4(pr->E[0], pr->g, pr->st));
   CK(launch_zero4(pr->E[1], pr->g, pr->st));
   return device_sync(pr, "kernel autotune");
@@ -487,6 +512,7 @@ pm_status pm_problem_destroy(pm_problem* pr) {
   if (!pr) return PM_OK;
   if (pr->st) cudaStreamSynchronize(pr->st);
   zmarch_destroy(pr->zp);
+  brick_destroy(pr->bp);
   cudaFree(pr->codes_base);
   cudaFree(pr->list);
   cudaFree(pr->f64_base[0]);

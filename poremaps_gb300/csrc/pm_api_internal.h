@@ -5,6 +5,7 @@
 
 #include "../../include/poremaps.h"
 #include "pm_internal.h"
+#include "pm_brick.h"
 #include "pm_zmarch.h"
 
 // One device-resident domain (the state behind a pm_problem handle).
@@ -34,6 +35,7 @@ struct pm_problem {
   size_t scratch_bytes = 0;
   int coop_blocks = 0;
   pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
+  pm::BrickPlan* bp = nullptr;   // TMA brick plan of the mixed form
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
   int brick[3] = {0, 0, 0};      // fluid-list order: bricks (0 = lexicographic rows)
   // state

@@ -15,32 +15,52 @@ namespace {
 
 __device__ __forceinline__ const SampleDesc& desc_of(const SampleDesc* d, int s) { return d[s]; }
 
+// Every thread block walks work items with a grid stride.  The item's sample
+// descriptor is staged in shared memory once per item (the voxel loop then
+// reads it with broadcast loads instead of re-reading global memory per
+// voxel), and each thread loads its next fluid-list entry before it computes
+// the current voxel.
 template <typename F>
-__device__ __forceinline__ void walk_items(const WorkItem* items, int nitems, F f) {
+__device__ __forceinline__ void walk_items(const SampleDesc* d, const WorkItem* items, int nitems,
+                                           F f) {
+  __shared__ __align__(16) SampleDesc sd;
+  static_assert(sizeof(SampleDesc) % 4 == 0, "descriptor copied as words");
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const WorkItem w = items[it];
-    for (int q = threadIdx.x; q < w.count; q += blockDim.x) f(w.sample, w.start + q);
+    __syncthreads();  // every reader of the previous item's descriptor is done
+    const int* src = reinterpret_cast<const int*>(d + w.sample);
+    for (int i = threadIdx.x; i < (int)(sizeof(SampleDesc) / 4); i += blockDim.x)
+      reinterpret_cast<int*>(&sd)[i] = src[i];
+    __syncthreads();
+    const int* list = sd.list + w.start;
+    int q = threadIdx.x;
+    int lin = q < w.count ? __ldg(list + q) : 0;
+    for (; q < w.count; q += blockDim.x) {
+      const int qn = q + blockDim.x;
+      const int next = qn < w.count ? __ldg(list + qn) : 0;
+      f(sd, lin);
+      lin = next;
+    }
   }
 }
 
 __global__ void k_batch_residual(const SampleDesc* d, const WorkItem* items, int nitems) {
-  walk_items(items, nitems, [&](int s, int q) {
-    const SampleDesc& sd = desc_of(d, s);
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
     float4* E = sd.ecur0 ? sd.E1 : sd.E0;
-    int lin = sd.list[q];
     if (sd.solver == 3) dc_residual_voxel<3>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
     else if (sd.solver == 2) dc_residual_voxel<2>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
     else dc_residual_voxel<1>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
   });
 }
 
-__global__ void k_batch_inner(const SampleDesc* d, const WorkItem* items, int nitems, int round) {
-  walk_items(items, nitems, [&](int s, int q) {
-    const SampleDesc& sd = desc_of(d, s);
+// At most 64 registers (1024 resident threads per SM at any block size the
+// server tunes), as the single-problem sweep.
+__global__ void __launch_bounds__(512, 2)
+    k_batch_inner(const SampleDesc* d, const WorkItem* items, int nitems, int round) {
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
     const int a = (sd.ecur0 + round - 1) & 1;
     const float4* Ein = a ? sd.E1 : sd.E0;
     float4* Eout = a ? sd.E0 : sd.E1;
-    int lin = sd.list[q];
     if (sd.solver == 3) dc_inner_voxel<3>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
     else if (sd.solver == 2) dc_inner_voxel<2>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
     else dc_inner_voxel<1>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
@@ -49,21 +69,18 @@ __global__ void k_batch_inner(const SampleDesc* d, const WorkItem* items, int ni
 
 __global__ void k_batch_correct(const SampleDesc* d, const WorkItem* items, int nitems,
                                 int rounds) {
-  walk_items(items, nitems, [&](int s, int q) {
-    const SampleDesc& sd = desc_of(d, s);
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
     const int a = (sd.ecur0 + rounds - 1) & 1;
-    dc_correct_voxel(sd.X0, a ? sd.E1 : sd.E0, sd.g, sd.list[q]);
+    dc_correct_voxel(sd.X0, a ? sd.E1 : sd.E0, sd.g, lin);
   });
 }
 
 __global__ void k_batch_sweep64(const SampleDesc* d, const WorkItem* items, int nitems,
                                 int round) {
-  walk_items(items, nitems, [&](int s, int q) {
-    const SampleDesc& sd = desc_of(d, s);
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
     const int a = (sd.xcur0 + round) & 1;
     const Fields<double>& A = a ? sd.X1 : sd.X0;
     const Fields<double>& B = a ? sd.X0 : sd.X1;
-    int lin = sd.list[q];
     if (sd.solver == 3) sweep64_voxel<3, 0, false>(A, B, sd.codes, sd.g, lin);
     else if (sd.solver == 2) sweep64_voxel<2, 0, false>(A, B, sd.codes, sd.g, lin);
     else sweep64_voxel<1, 0, false>(A, B, sd.codes, sd.g, lin);

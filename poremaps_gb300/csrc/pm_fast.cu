@@ -112,6 +112,52 @@ __global__ void __launch_bounds__(256, 4) k_dc_inner_occ(const float4* E, float4
     dc_inner_voxel<SOLVER>(E, E2, R, codes, g, list[q]);
 }
 
+// Persistent form of the fluid-list sweep: one wave of CTAs (MINB per SM)
+// walks the list with a grid stride, and every thread loads its next list
+// entry before it computes the current voxel, so the list read's latency
+// overlaps the stencil instead of preceding it.
+template <int SOLVER, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_dc_inner_pf(const float4* E, float4* E2,
+                                                          const float4* R, const uint8_t* codes,
+                                                          const int* list, int nlist, Grid g) {
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  int lin = q < nlist ? __ldg(list + q) : 0;
+  for (; q < nlist; q += stride) {
+    const int qn = q + stride;
+    const int next = qn < nlist ? __ldg(list + qn) : 0;
+    dc_inner_voxel<SOLVER>(E, E2, R, codes, g, lin);
+    lin = next;
+  }
+}
+
+template <int MINB>
+static cudaError_t launch_pf(const float4* e, float4* e2, const float4* r, const uint8_t* codes,
+                             const int* list, int nlist, const Grid& g, int solver,
+                             cudaStream_t st) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int blocks = (nlist + 255) / 256;
+  if (blocks < 1) return cudaSuccess;
+  if (blocks > MINB * sms) blocks = MINB * sms;
+  if (solver == 1) k_dc_inner_pf<1, MINB><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  else if (solver == 2) k_dc_inner_pf<2, MINB><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  else k_dc_inner_pf<3, MINB><<<blocks, 256, 0, st>>>(e, e2, r, codes, list, nlist, g);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dc_inner_pf(const float4* e, float4* e2, const float4* r,
+                               const uint8_t* codes, const int* list, int nlist, const Grid& g,
+                               int solver, int minb, cudaStream_t st) {
+  if (minb >= 5) return launch_pf<5>(e, e2, r, codes, list, nlist, g, solver, st);
+  return launch_pf<4>(e, e2, r, codes, list, nlist, g, solver, st);
+}
+
 cudaError_t launch_dc_inner_occ(const float4* e, float4* e2, const float4* r,
                                 const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                 int solver, cudaStream_t st) {

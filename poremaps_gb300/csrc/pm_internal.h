@@ -104,6 +104,11 @@ cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uin
 cudaError_t launch_dc_inner(const float4* e, float4* e2, const float4* r, const uint8_t* codes,
                             const int* list, int nlist, const Grid& g, int solver,
                             cudaStream_t st);
+// Persistent fluid-list sweep (one wave of minb CTAs per SM, list entries
+// prefetched one iteration ahead); minb 4 or 5.
+cudaError_t launch_dc_inner_pf(const float4* e, float4* e2, const float4* r,
+                               const uint8_t* codes, const int* list, int nlist, const Grid& g,
+                               int solver, int minb, cudaStream_t st);
 cudaError_t launch_dc_inner_occ(const float4* e, float4* e2, const float4* r,
                                 const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                 int solver, cudaStream_t st);

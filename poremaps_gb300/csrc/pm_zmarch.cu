@@ -15,10 +15,8 @@
 // Every mbarrier wait is bounded (clock64 budget); on expiry the CTA records
 // an error code, drains its own copies still in flight (again bounded) and
 // returns, so a broken pipeline never hangs the device.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include "pm_stencil.cuh"
+#include "pm_tma.cuh"
 #include "pm_zmarch.h"
 
 namespace pm {
@@ -59,48 +57,13 @@ struct Smem {
 using TileA = Tile<32, 16>;
 using TileB = Tile<32, 8>;
 
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect(unsigned long long* b, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(unsigned long long* b, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: false once about `budget` clock cycles have passed.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity,
-                                          long long budget) {
-  long long t0 = clock64();
-  for (unsigned i = 0;; ++i) {
-    if (mbar_try(b, parity)) return true;
-    if ((i & 255) == 255 && clock64() - t0 > budget) return false;
-  }
-}
+using tma::mbar_expect;
+using tma::mbar_init;
+using tma::mbar_wait;
 
 __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int x, int y, int z,
                                           unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-      "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-      : "memory");
+  tma::load3(dst, map, x, y, z, bar);
 }
 
 struct Maps {
@@ -141,7 +104,7 @@ __global__ void __launch_bounds__(T::THREADS)
   if (leader) {
     for (int i = 0; i < NR; ++i) mbar_init(&S.bar[i], 1);
     mbar_init(&S.bar_pro, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tma::fence_mbar_init();
   }
   __syncthreads();
   if (leader) {
@@ -242,6 +205,10 @@ __global__ void __launch_bounds__(T::THREADS)
   }
 }
 
+}  // namespace
+
+namespace tma {
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -255,21 +222,21 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D map over a padded array: dims {pitch elements, NY, NZ}.
+// 3-D map over a padded array: dims {pitch elements, NY, NZ}, box {bx, by, bz}.
 bool encode(CUtensorMap* m, CUtensorMapDataType t, int esize, void* base, const Grid& g,
-            long long pitch, unsigned bx, unsigned by) {
+            long long pitch, unsigned bx, unsigned by, unsigned bz) {
   auto fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)g.NY, (cuuint64_t)g.NZ};
   cuuint64_t strides[2] = {(cuuint64_t)pitch * esize, (cuuint64_t)pitch * g.NY * esize};
-  cuuint32_t box[3] = {bx, by, 1};
+  cuuint32_t box[3] = {bx, by, bz};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(m, t, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-}  // namespace
+}  // namespace tma
 
 struct ZmarchPlan {
   Maps maps[2];  // source buffer E0 / E1
@@ -279,7 +246,7 @@ struct ZmarchPlan {
   dim3 grid;
 };
 
-int zmarch_available() { return encode_fn() != nullptr; }
+int zmarch_available() { return tma::encode_fn() != nullptr; }
 
 template <class T>
 static void set_smem_attr() {
@@ -305,12 +272,12 @@ cudaError_t zmarch_create(ZmarchPlan** out, const Grid& g, float4* E0, float4* E
   float4* src[2] = {E0, E1};
   bool ok = true;
   for (int b = 0; b < 2; ++b) {
-    ok &= encode(&pl->maps[b].e, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src[b] - kXoff4, g,
-                 4LL * g.px4, 4 * (TX + 4), TY + 4);
-    ok &= encode(&pl->maps[b].r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, R - kXoff4, g, 4LL * g.px4,
-                 4 * TX, TY);
-    ok &= encode(&pl->maps[b].codes, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, (void*)(codes - kXoffC),
-                 g, g.pxc, TX, TY);
+    ok &= tma::encode(&pl->maps[b].e, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src[b] - kXoff4, g,
+                      4LL * g.px4, 4 * (TX + 4), TY + 4, 1);
+    ok &= tma::encode(&pl->maps[b].r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, R - kXoff4, g,
+                      4LL * g.px4, 4 * TX, TY, 1);
+    ok &= tma::encode(&pl->maps[b].codes, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1,
+                      (void*)(codes - kXoffC), g, g.pxc, TX, TY, 1);
   }
   if (!ok) {
     delete pl;

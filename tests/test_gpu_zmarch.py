@@ -1,10 +1,12 @@
-"""The TMA z-march FP32 correction sweep against the fluid-list kernel.
+"""The TMA-fed FP32 correction sweeps (z-march, bricks) against the
+fluid-list kernel.
 
-Both run the same per-voxel arithmetic (update_fast<float> + residual), one
-reading the stencil from shared-memory planes streamed by TMA, the other from
-global memory, so the mixed form must give bitwise identical fields with
-either kernel -- on sizes that are not multiples of the 32 x 16 tile, short z
-extents, every boundary family and every solver the mixed form supports.
+All run the same per-voxel arithmetic (update_fast<float> + residual), the
+TMA kernels reading the stencil from shared-memory planes or bricks, the
+fluid-list kernels from global memory, so the mixed form must give bitwise
+identical fields with every kernel -- on sizes that are not multiples of the
+tiles or bricks, short z extents, every boundary family and every solver the
+mixed form supports.
 """
 import numpy as np
 import pytest
@@ -19,12 +21,15 @@ CASES = [((20, 20, 20), 0, 2), ((13, 37, 45), 1, 2), ((5, 17, 33), 2, 3), ((40, 
 
 
 @pytest.mark.parametrize("shape,bc,solver", CASES)
-def test_zmarch_equals_fluid_list(shape, bc, solver):
+def test_tma_kernels_equal_fluid_list(shape, bc, solver):
     g = synth.random_solid(shape, 0.3, sum(shape) + bc)
     out = []
-    for kernel in (1, 0, 3, 2):
+    for kernel, brick in ((1, (0, 0, 0)), (0, (0, 0, 0)), (3, (0, 0, 0)), (2, (32, 8, 8)),
+                          (4, (32, 8, 8)), (4, (32, 8, 4)), (4, (32, 4, 4)), (5, (0, 0, 0)),
+                          (6, (32, 8, 8))):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=solver, order="jacobi",
-                        precision="mixed", kernel=kernel, mixed_inner=40) as p:
+                        precision="mixed", kernel=kernel, brick=brick, mixed_inner=40) as p:
+            assert p.kernel() == kernel and p.brick() == brick
             p.iterate(117)
             out.append(p.fields())
     for other in out[1:]:
@@ -35,7 +40,7 @@ def test_zmarch_equals_fluid_list(shape, bc, solver):
 def test_autotuned_kernel_is_a_candidate():
     g = synth.random_solid((32, 32, 32), 0.3, 1)
     with pm.Problem(g, None, solving_algorithm=2, order="jacobi", precision="mixed") as p:
-        assert p.kernel() in (0, 1, 2, 3)
+        assert p.kernel() in (0, 1, 2, 3, 4, 5, 6)
 
 
 @pytest.mark.parametrize("shape,bc", [((40, 36, 70), 0), ((33, 21, 50), 2)])
