@@ -187,6 +187,13 @@ pm_status pm_problem_reset(pm_problem* pr);
  * from before the first sweep to after the reduction's read-back. */
 pm_status pm_block_timed(pm_problem* pr, int n, int check, double* permeability, double* conv,
                          double* device_ms);
+/* pm_block_timed for `count` problems at once: each problem's n iterations
+ * (and check) are issued on its own stream so the blocks run concurrently;
+ * *device_ms = CUDA-event time from a start event every stream waits on to an
+ * end event that waits on every stream.  permeability/conv: arrays of count.
+ * No counterpart in the reference. */
+pm_status pm_block_group_timed(pm_problem** prs, int count, int n, int check,
+                               double* permeability, double* conv, double* device_ms);
 /* Average device time of one launch of a sweep kernel of this problem's form,
  * measured with CUDA events over n back-to-back launches on its stream
  * (kernel 0: the form's main sweep -- the FP32 correction sweep of the mixed

@@ -82,7 +82,7 @@ EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
            "pm_get_iteration", "pm_get_fields", "pm_set_fields", "pm_resume_outputs",
            "pm_get_neighborhood", "pm_write_outputs",
            "pm_run_inp", "pm_solve_tensor", "pm_set_device", "pm_problem_reset",
-           "pm_block_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_get_brick", "pm_reduce_fields_noalloc",
+           "pm_block_timed", "pm_block_group_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_get_brick", "pm_reduce_fields_noalloc",
            "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms"]
@@ -126,6 +126,8 @@ def load_library(path: str = LIB_PATH):
         "pm_problem_reset": (C.c_int, [vp]),
         "pm_block_timed": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
                                      P(C.c_double)]),
+        "pm_block_group_timed": (C.c_int, [P(vp), C.c_int, C.c_int, C.c_int, P(C.c_double),
+                                           P(C.c_double), P(C.c_double)]),
         "pm_kernel_time": (C.c_int, [vp, C.c_int, C.c_int, P(C.c_double)]),
         "pm_kernel_launches": (C.c_uint64, []),
         "pm_get_kernel": (C.c_int, [vp, P(C.c_int)]),
@@ -306,6 +308,18 @@ class Problem:
 
 def set_device(device: int) -> None:
     _check(load_library().pm_set_device(device))
+
+
+def block_group_timed(problems, n: int, check: bool = True, permeability=None):
+    """One block of n iterations of every problem, concurrently on their
+    streams; returns (device_ms, conv list, permeability list)."""
+    m = len(problems)
+    hs = (C.c_void_p * m)(*[p.h for p in problems])
+    k = (C.c_double * m)(*(permeability or [0.0] * m))
+    conv = (C.c_double * m)()
+    ms = C.c_double()
+    _check(load_library().pm_block_group_timed(hs, m, n, int(check), k, conv, C.byref(ms)))
+    return ms.value, list(conv), list(k)
 
 
 def kernel_launches() -> int:

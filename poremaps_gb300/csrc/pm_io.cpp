@@ -8,6 +8,7 @@
 #include <string.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <string>
 #include <thread>
 #include <vector>
@@ -36,6 +37,29 @@ pm_status write_raw(const std::string& path, const void* data, size_t bytes) {
   }
   close(fd);
   return PM_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Geometry of the run with flow along x (axis 0: z' = x, y' = z, x' = y) or
+// along y (axis 1: z' = y, y' = x, x' = z), README.md:221-225; arrays are
+// x fastest.  Tiled so both the reads and the writes stay in cache.
+void rotate_geometry(const uint8_t* g, int nx, int ny, int nz, int axis, uint8_t* out) {
+  const int T = 16;
+  for (int z0 = 0; z0 < nz; z0 += T)
+    for (int y0 = 0; y0 < ny; y0 += T)
+      for (int x0 = 0; x0 < nx; x0 += T) {
+        const int z1 = std::min(z0 + T, nz), y1 = std::min(y0 + T, ny), x1 = std::min(x0 + T, nx);
+        for (int z = z0; z < z1; ++z)
+          for (int y = y0; y < y1; ++y)
+            for (int x = x0; x < x1; ++x) {
+              const uint8_t v = g[((size_t)z * ny + y) * nx + x];
+              if (axis == 0) out[((size_t)x * nz + z) * ny + y] = v;  // (ny, nz, nx)
+              else out[((size_t)y * nx + x) * nz + z] = v;             // (nz, nx, ny)
+            }
+      }
 }
 
 }  // namespace
@@ -185,43 +209,40 @@ pm_status pm_solve_tensor(const pm_params* p, const uint8_t* geom, double K[9],
                           pm_result res3[3]) {
   if (!p || !geom || !K) return set_error(PM_ERR_INVALID, "bad arguments");
   const int nx = p->size[0], ny = p->size[1], nz = p->size[2];
-  const size_t n = (size_t)nx * ny * nz;
-  std::vector<uint8_t> gx(n), gy(n);
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y)
-      for (int x = 0; x < nx; ++x) {
-        uint8_t v = geom[((size_t)z * ny + y) * nx + x];
-        // flow along x: z' = x, y' = z, x' = y; sizes (nx', ny', nz') = (ny, nz, nx)
-        gx[((size_t)x * nz + z) * ny + y] = v;
-        // flow along y: z' = y, y' = x, x' = z; sizes (nx', ny', nz') = (nz, nx, ny)
-        gy[((size_t)y * nx + x) * nz + z] = v;
-      }
-  pm_params px = *p, py = *p, pz = *p;
-  px.size[0] = ny; px.size[1] = nz; px.size[2] = nx;
-  py.size[0] = nz; py.size[1] = nx; py.size[2] = ny;
-  pm_params* ps[3] = {&px, &py, &pz};
-  const uint8_t* gs[3] = {gx.data(), gy.data(), geom};
+  if (nx < 1 || ny < 1 || nz < 1) return set_error(PM_ERR_INVALID, "bad size");
+  pm_params ps[3] = {*p, *p, *p};
+  // flow along x: sizes (nx', ny', nz') = (ny, nz, nx); along y: (nz, nx, ny)
+  ps[0].size[0] = ny; ps[0].size[1] = nz; ps[0].size[2] = nx;
+  ps[1].size[0] = nz; ps[1].size[1] = nx; ps[1].size[2] = ny;
   for (int a = 0; a < 3; ++a) {
-    ps[a]->write_log = 0;
-    memset(ps[a]->dom_interest, 0, sizeof(ps[a]->dom_interest));
+    ps[a].write_log = 0;
+    memset(ps[a].dom_interest, 0, sizeof(ps[a].dom_interest));
   }
   pm_result r[3];
   pm_status st[3] = {PM_OK, PM_OK, PM_OK};
-  pm_problem* pr[3] = {nullptr, nullptr, nullptr};
-  for (int a = 0; a < 3; ++a) {
-    st[a] = pm_problem_create(ps[a], gs[a], &pr[a]);
-    if (st[a] != PM_OK) {
-      for (int b = 0; b < a; ++b) pm_problem_destroy(pr[b]);
-      return st[a];
+  std::string err[3];
+  // The three solves are independent: each host thread rotates its copy of
+  // the geometry, creates its problem (own stream) and solves it, so the
+  // rotations, set-up and sweeps of the three axes overlap.
+  auto run = [&](int a) {
+    std::vector<uint8_t> rot;
+    const uint8_t* g = geom;
+    if (a < 2) {
+      rot.resize((size_t)nx * ny * nz);
+      rotate_geometry(geom, nx, ny, nz, a, rot.data());
+      g = rot.data();
     }
-  }
-  // the three solves are independent: run them concurrently on their streams
+    pm_problem* pr = nullptr;
+    st[a] = pm_problem_create(&ps[a], g, &pr);
+    if (st[a] == PM_OK) st[a] = pm_solve(pr, &r[a]);
+    if (st[a] != PM_OK) err[a] = pm_last_error();
+    pm_problem_destroy(pr);
+  };
   std::vector<std::thread> th;
-  for (int a = 0; a < 3; ++a) th.emplace_back([&, a] { st[a] = pm_solve(pr[a], &r[a]); });
+  for (int a = 0; a < 3; ++a) th.emplace_back(run, a);
   for (auto& t : th) t.join();
-  for (int a = 0; a < 3; ++a) pm_problem_destroy(pr[a]);
   for (int a = 0; a < 3; ++a)
-    if (st[a] != PM_OK && st[a] != PM_ERR_NONFINITE) return st[a];
+    if (st[a] != PM_OK && st[a] != PM_ERR_NONFINITE) return set_error(st[a], "%s", err[a].c_str());
   // K[3*i + j]: response along axis i to the pressure drop along axis j
   K[3 * 1 + 0] = r[0].wk13; K[3 * 2 + 0] = r[0].wk23; K[3 * 0 + 0] = r[0].wk33;
   K[3 * 2 + 1] = r[1].wk13; K[3 * 0 + 1] = r[1].wk23; K[3 * 1 + 1] = r[1].wk33;
@@ -229,7 +250,7 @@ pm_status pm_solve_tensor(const pm_params* p, const uint8_t* geom, double K[9],
   if (res3)
     for (int a = 0; a < 3; ++a) res3[a] = r[a];
   for (int a = 0; a < 3; ++a)
-    if (st[a] != PM_OK) return st[a];
+    if (st[a] != PM_OK) return set_error(st[a], "%s", err[a].c_str());
   return PM_OK;
 }
 
