@@ -371,7 +371,8 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
            2: ("k_dc_inner_occ", "fluid-list FP32 correction sweep, 4 blocks/SM"),
            4: ("k_brick_inner", "TMA brick tiles, FP32 correction sweep"),
            5: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 4 blocks/SM"),
-           6: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 5 blocks/SM")}
+           6: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 3 blocks/SM"),
+           7: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 2 blocks/SM")}
 
 
 def run_profile_case(args):

@@ -96,14 +96,14 @@ typedef struct {
   int write_log;                /* 1: append the reference log rows to log_file_name */
   int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
   int kernel;                   /* correction sweep of the mixed form: -1 autotune
-                                   (default: time the fluid-list kernels 5, 2, 1 in a
-                                   few list orders on the problem, keep the fastest),
+                                   (default: time the fluid-list kernels 6, 5, 7, 2 on
+                                   the problem, keep the fastest),
                                    0 TMA z-march 32x16 tiles, 3 TMA
                                    z-march 32x8 tiles, 1 fluid-list gather, 2 fluid-list
                                    gather at four blocks per SM, 4 TMA bricks (one
-                                   brick + halo per CTA in shared memory), 5 / 6
+                                   brick + halo per CTA in shared memory), 5 / 6 / 7
                                    persistent fluid-list gather, list prefetched, at
-                                   four / five blocks per SM */
+                                   four / three / two blocks per SM */
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */

@@ -85,7 +85,7 @@ pm_status validate(const pm_params* p) {
     if (!none && !all)
       return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
   }
-  if (p->kernel < -1 || p->kernel > 6) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel < -1 || p->kernel > 7) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
   if (p->kernel == 4 && p->brick[0] && pm::brick_shape_of(p->brick[0], p->brick[1], p->brick[2]) < 0)
     return set_error(PM_ERR_INVALID, "kernel 4 bricks are 32x8x8, 32x8x4 or 32x4x4");
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
@@ -119,9 +119,9 @@ pm_status correction_sweep(pm_problem* pr, int src) {
     CK(zmarch_inner(pr->zp, src, pr->E[1 - src], pr->g, pr->solver, pr->st));
   } else if (pr->bp) {
     CK(brick_inner(pr->bp, src, pr->E[1 - src], pr->R, pr->list, pr->g, pr->solver, pr->st));
-  } else if (pr->kern == 5 || pr->kern == 6) {
+  } else if (pr->kern >= 5) {
     CK(launch_dc_inner_pf(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist,
-                          pr->g, pr->solver, pr->kern == 6 ? 5 : 4, pr->st));
+                          pr->g, pr->solver, 9 - pr->kern, pr->st));
   } else if (pr->kern == 2) {
     CK(launch_dc_inner_occ(pr->E[src], pr->E[1 - src], pr->R, pr->codes, pr->list, pr->nlist,
                            pr->g, pr->solver, pr->st));
@@ -151,8 +151,9 @@ pm_status iterate64(pm_problem* pr) {
 // Correction-sweep kernels of the mixed form: 0 TMA z-march with 32 x 16
 // tiles, 3 the same with 32 x 8 tiles, 1 fluid-list gather, 2 fluid-list
 // gather compiled for four blocks per SM, 4 TMA bricks (32x8x8, 32x8x4 or
-// 32x4x4 voxels per CTA, the fluid list in the same brick order), 5 and 6
-// persistent fluid-list gather with the list prefetched (4 / 5 CTAs per SM).
+// 32x4x4 voxels per CTA, the fluid list in the same brick order), 5,
+// 6 and 7 persistent fluid-list gather with the list prefetched (4 / 3 / 2
+// CTAs per SM).
 // kernel < 0 times the fluid-list candidates on this problem (a few launches
 // each; the correction buffers are scratch until the first residual sweep)
 // and keeps the fastest.
@@ -204,11 +205,11 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     if (s != PM_OK) return s;
     return device_sync(pr, "kernel choice");
   }
-  // The TMA kernels (0, 3, 4) and kernel 6 lose on every medium measured so
-  // far and are left to explicit choice; timing them would only lengthen the
-  // set-up of every problem.
-  const Cand cands[] = {{5, {0, 0, 0}}, {5, {32, 8, 8}}, {5, {32, 4, 4}}, {2, {0, 0, 0}},
-                        {1, {32, 8, 8}}};
+  // The TMA kernels (0, 3, 4) lose on every medium measured so far and are
+  // left to explicit choice; timing them would only lengthen the set-up of
+  // every problem.
+  const Cand cands[] = {{6, {0, 0, 0}}, {6, {32, 8, 8}}, {5, {0, 0, 0}}, {7, {0, 0, 0}},
+                        {2, {0, 0, 0}}};
   const int nc = 5;
   // Each candidate: the best of three timings of five sweeps.  The first
   // candidate is kept unless another one is at least 2 % faster, so timing

@@ -28,8 +28,10 @@ enum { kBatchResidual = 0, kBatchInner = 1, kBatchCorrect = 2, kBatchSweep64 = 3
 
 // kind: kBatch*; round: sweep index inside the block (inner / sweep64), the
 // number of rounds (correct), or the state parity (sumw).  blocks <= 0: one
-// block per item.
+// block per item.  solver: the solver all samples use (1..3; a kernel
+// specialised for it), or 0 when they differ.
 cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, int nitems,
-                         int round, int threads, int blocks, double* out, cudaStream_t st);
+                         int round, int threads, int blocks, double* out, cudaStream_t st,
+                         int solver = 0);
 
 }  // namespace pm

@@ -115,7 +115,10 @@ __global__ void __launch_bounds__(256, 4) k_dc_inner_occ(const float4* E, float4
 // Persistent form of the fluid-list sweep: one wave of CTAs (MINB per SM)
 // walks the list with a grid stride, and every thread loads its next list
 // entry before it computes the current voxel, so the list read's latency
-// overlaps the stencil instead of preceding it.
+// overlaps the stencil instead of preceding it.  MINB 3 leaves each thread
+// ~80 registers: all 13 float4 gathers of a voxel stay in flight at once
+// (at 64 registers the compiler splits them and spills), which is worth more
+// than the extra warps of MINB 4.
 template <int SOLVER, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_dc_inner_pf(const float4* E, float4* E2,
                                                           const float4* R, const uint8_t* codes,
@@ -154,7 +157,8 @@ static cudaError_t launch_pf(const float4* e, float4* e2, const float4* r, const
 cudaError_t launch_dc_inner_pf(const float4* e, float4* e2, const float4* r,
                                const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                int solver, int minb, cudaStream_t st) {
-  if (minb >= 5) return launch_pf<5>(e, e2, r, codes, list, nlist, g, solver, st);
+  if (minb <= 2) return launch_pf<2>(e, e2, r, codes, list, nlist, g, solver, st);
+  if (minb == 3) return launch_pf<3>(e, e2, r, codes, list, nlist, g, solver, st);
   return launch_pf<4>(e, e2, r, codes, list, nlist, g, solver, st);
 }
 

@@ -105,7 +105,7 @@ cudaError_t launch_dc_inner(const float4* e, float4* e2, const float4* r, const 
                             const int* list, int nlist, const Grid& g, int solver,
                             cudaStream_t st);
 // Persistent fluid-list sweep (one wave of minb CTAs per SM, list entries
-// prefetched one iteration ahead); minb 4 or 5.
+// prefetched one iteration ahead); minb 4, 3 or 2.
 cudaError_t launch_dc_inner_pf(const float4* e, float4* e2, const float4* r,
                                const uint8_t* codes, const int* list, int nlist, const Grid& g,
                                int solver, int minb, cudaStream_t st);

@@ -79,6 +79,7 @@ struct pm_server {
   cudaGraphExec_t gexec = nullptr;
   int graph_kernels = 0;
   int threads = 256, chunk = 8192;
+  int solver = 0;  // the solver every resident sample uses, 0 when they differ
   long long tuned_for = -1;
   double busy_ms = 0.0;
   unsigned long long lups = 0;
@@ -178,8 +179,22 @@ pm_status admit(pm_server* s) {
   return PM_OK;
 }
 
+// Work items of at most `chunk` fluid voxels, and small enough that a round
+// has at least ~8 items per SM: when a few samples remain (the slow ones of a
+// batch) the device still gets a full grid.
 void build_items(pm_server* s, int chunk) {
   s->h_items.clear();
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  long long total = 0;
+  for (auto& r : s->res) total += r.pr->nlist;
+  const long long fill = (total + 8LL * sms - 1) / (8LL * sms);
+  chunk = (int)std::max(512LL, std::min<long long>(chunk, fill));
   for (size_t i = 0; i < s->res.size(); ++i) {
     Res& r = s->res[i];
     r.item0 = (int)s->h_items.size();
@@ -218,16 +233,19 @@ pm_status issue_block(pm_server* s, int* nk) {
   const int n = (int)s->h_items.size(), T = s->threads;
   int k = 0;
   if (mixed(s)) {
-    SCK(launch_batch(kBatchResidual, s->d_desc, s->d_items, n, 0, T, 0, nullptr, s->st));
+    SCK(launch_batch(kBatchResidual, s->d_desc, s->d_items, n, 0, T, 0, nullptr, s->st,
+                     s->solver));
     ++k;
     for (int r = 1; r < s->block; ++r, ++k)
-      SCK(launch_batch(kBatchInner, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st));
+      SCK(launch_batch(kBatchInner, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st,
+                       s->solver));
     SCK(launch_batch(kBatchCorrect, s->d_desc, s->d_items, n, s->block, T, 0, nullptr, s->st));
     SCK(launch_batch(kBatchSumW, s->d_desc, s->d_items, n, 0, T, 0, s->d_part, s->st));
     k += 2;
   } else {
     for (int r = 0; r < s->block; ++r, ++k)
-      SCK(launch_batch(kBatchSweep64, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st));
+      SCK(launch_batch(kBatchSweep64, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st,
+                       s->solver));
     SCK(launch_batch(kBatchSumW, s->d_desc, s->d_items, n, s->block, T, 0, s->d_part, s->st));
     ++k;
   }
@@ -253,11 +271,11 @@ pm_status autotune(pm_server* s) {
     if (e != PM_OK) return e;
     for (int t : kThreads) {
       SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
-                       s->st));
+                       s->st, s->solver));
       SCK(cudaEventRecord(s->e0, s->st));
       for (int i = 0; i < 3; ++i)
         SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
-                         s->st));
+                         s->st, s->solver));
       SCK(cudaEventRecord(s->e1, s->st));
       SCK(cudaEventSynchronize(s->e1));
       float ms = 0.f;
@@ -273,6 +291,9 @@ pm_status autotune(pm_server* s) {
 
 pm_status rebuild(pm_server* s) {
   s->h_desc.clear();
+  s->solver = s->res.empty() ? 0 : s->res[0].pr->solver;
+  for (auto& r : s->res)
+    if (r.pr->solver != s->solver) s->solver = 0;
   for (auto& r : s->res) {
     pm_problem* pr = r.pr;
     SampleDesc d;

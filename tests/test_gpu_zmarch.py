@@ -26,7 +26,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
     out = []
     for kernel, brick in ((1, (0, 0, 0)), (0, (0, 0, 0)), (3, (0, 0, 0)), (2, (32, 8, 8)),
                           (4, (32, 8, 8)), (4, (32, 8, 4)), (4, (32, 4, 4)), (5, (0, 0, 0)),
-                          (6, (32, 8, 8))):
+                          (6, (32, 8, 8)), (7, (0, 0, 0))):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=solver, order="jacobi",
                         precision="mixed", kernel=kernel, brick=brick, mixed_inner=40) as p:
             assert p.kernel() == kernel and p.brick() == brick
@@ -40,7 +40,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
 def test_autotuned_kernel_is_a_candidate():
     g = synth.random_solid((32, 32, 32), 0.3, 1)
     with pm.Problem(g, None, solving_algorithm=2, order="jacobi", precision="mixed") as p:
-        assert p.kernel() in (0, 1, 2, 3, 4, 5, 6)
+        assert p.kernel() in (0, 1, 2, 3, 4, 5, 6, 7)
 
 
 @pytest.mark.parametrize("shape,bc", [((40, 36, 70), 0), ((33, 21, 50), 2)])
