@@ -139,10 +139,10 @@ pm_status iterate64(pm_problem* pr) {
     CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
                       pr->st));
   } else {
-    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 1,
+    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nred, pr->g, pr->solver, pr->exact, 1,
                       pr->st));
-    CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 2,
-                      pr->st));
+    CK(launch_sweep64(A, B, pr->codes, pr->list + pr->nred, pr->nlist - pr->nred, pr->g,
+                      pr->solver, pr->exact, 2, pr->st));
   }
   pr->cur = 1 - pr->cur;
   return PM_OK;
@@ -512,6 +512,19 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   CKF(launch_copy_fields64(pr->F[1], pr->F[0], g, pr->st));
   CKF(cudaStreamSynchronize(pr->st));
   pr->nlist = *(int*)pr->hout;
+  if (pr->order == PM_ORDER_REDBLACK) {
+    // red voxels first, then black: each half-sweep walks only its own colour
+    int* dc = (int*)pr->dout;
+    CKF(launch_fluid_list(pr->codes, g, pr->list, dc, pr->st, 0, 0, 0, 0));
+    CKF(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(int), cudaMemcpyDeviceToHost, pr->st));
+    CKF(cudaStreamSynchronize(pr->st));
+    pr->nred = *(int*)pr->hout;
+    CKF(launch_fluid_list(pr->codes, g, pr->list + pr->nred, dc, pr->st, 0, 0, 0, 1));
+    CKF(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(int), cudaMemcpyDeviceToHost, pr->st));
+    CKF(cudaStreamSynchronize(pr->st));
+    if (pr->nred + *(int*)pr->hout != pr->nlist)
+      return fail(set_error(PM_ERR_CUDA, "red-black fluid lists do not add up"));
+  }
   if (pr->precision == PM_PREC_MIXED) {
     pm_status ts = choose_correction_kernel(pr, p->kernel);
     if (ts != PM_OK) return fail(ts);
@@ -734,10 +747,10 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
         CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
                           pr->st));
       } else {
-        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 1,
+        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nred, pr->g, pr->solver, pr->exact, 1,
                           pr->st));
-        CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 2,
-                          pr->st));
+        CK(launch_sweep64(A, B, pr->codes, pr->list + pr->nred, pr->nlist - pr->nred, pr->g,
+                          pr->solver, pr->exact, 2, pr->st));
       }
     }
   }

@@ -72,9 +72,11 @@ unsigned long long launches_total();
 // All launchers are asynchronous on `st` and return the launch error.
 cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st);
 // Fluid list in brick order (bx x by x bz bricks; bx <= 0: whole rows,
-// by/bz <= 0: 1, i.e. lexicographic order).
+// by/bz <= 0: 1, i.e. lexicographic order); parity 0 / 1 keeps only the
+// voxels with (x + y + z) of that parity, < 0 all of them.
 cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
-                              cudaStream_t st, int bx = 0, int by = 0, int bz = 0);
+                              cudaStream_t st, int bx = 0, int by = 0, int bz = 0,
+                              int parity = -1);
 cudaError_t launch_counts(const uint8_t* codes, const Grid& g, const int di[6],
                           unsigned long long* out4, cudaStream_t st);
 cudaError_t launch_init64(Fields<double> f, const uint8_t* codes, const Grid& g,

@@ -138,13 +138,20 @@ __device__ __forceinline__ void segment(const Grid& g, const Bricks& b, int s, i
   if (y >= g.ny || z >= g.nz) len = 0;
 }
 
-__global__ void k_seg_counts(const uint8_t* codes, Grid g, Bricks b, int* seg_count) {
+// parity < 0: every fluid voxel; 0 / 1: only those with (x + y + z) of that
+// parity (the red / black half of a red-black sweep).
+__device__ __forceinline__ bool keep(const uint8_t* c, int x, int x0, int y, int z, int parity) {
+  return c[x] != 0 && (parity < 0 || ((x0 + x + y + z) & 1) == parity);
+}
+
+__global__ void k_seg_counts(const uint8_t* codes, Grid g, Bricks b, int parity,
+                             int* seg_count) {
   int x0, len, y, z;
   segment(g, b, blockIdx.x, x0, len, y, z);
   int cnt = 0;
   if (len > 0) {
     const uint8_t* c = codes + ((long long)(z + 2) * g.NY + (y + 2)) * g.pxc + 2 + x0;
-    for (int x = threadIdx.x; x < len; x += blockDim.x) cnt += c[x] != 0;
+    for (int x = threadIdx.x; x < len; x += blockDim.x) cnt += keep(c, x, x0, y, z, parity);
   }
   __shared__ int s[32];
   for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -157,8 +164,8 @@ __global__ void k_seg_counts(const uint8_t* codes, Grid g, Bricks b, int* seg_co
   }
 }
 
-__global__ void k_seg_fill(const uint8_t* codes, Grid g, Bricks b, const int* seg_off,
-                           int* list) {
+__global__ void k_seg_fill(const uint8_t* codes, Grid g, Bricks b, int parity,
+                           const int* seg_off, int* list) {
   int x0, len, y, z;
   segment(g, b, blockIdx.x, x0, len, y, z);
   if (len <= 0) return;
@@ -167,7 +174,7 @@ __global__ void k_seg_fill(const uint8_t* codes, Grid g, Bricks b, const int* se
   const int lane = threadIdx.x;  // one warp walks the segment in x order
   for (int xs = 0; xs < len; xs += 32) {
     const int x = xs + lane;
-    const bool f = x < len && c[x] != 0;
+    const bool f = x < len && keep(c, x, x0, y, z, parity);
     const unsigned m = __ballot_sync(0xffffffffu, f);
     if (f)
       list[base + __popc(m & ((1u << lane) - 1))] =
@@ -202,7 +209,7 @@ __global__ void k_scan_rows(const int* row_count, int nrows, int* row_off, int* 
 }
 
 cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, int* count,
-                              cudaStream_t st, int bx, int by, int bz) {
+                              cudaStream_t st, int bx, int by, int bz, int parity) {
   Bricks b;
   b.bx = bx > 0 ? std::min(bx, g.nx) : g.nx;
   b.by = by > 0 ? std::min(by, g.ny) : 1;
@@ -215,9 +222,9 @@ cudaError_t launch_fluid_list(const uint8_t* codes, const Grid& g, int* list, in
   int* tmp = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&tmp, sizeof(int) * 2 * (size_t)nseg, st);
   if (e != cudaSuccess) return e;
-  k_seg_counts<<<(unsigned)nseg, 128, 0, st>>>(codes, g, b, tmp);
+  k_seg_counts<<<(unsigned)nseg, 128, 0, st>>>(codes, g, b, parity, tmp);
   k_scan_rows<<<1, 1024, 0, st>>>(tmp, (int)nseg, tmp + nseg, count);
-  k_seg_fill<<<(unsigned)nseg, 32, 0, st>>>(codes, g, b, tmp + nseg, list);
+  k_seg_fill<<<(unsigned)nseg, 32, 0, st>>>(codes, g, b, parity, tmp + nseg, list);
   count_launches(3);
   e = cudaGetLastError();
   cudaFreeAsync(tmp, st);

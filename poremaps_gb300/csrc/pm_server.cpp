@@ -127,6 +127,43 @@ void drop_graph(pm_server* s) {
   s->gexec = nullptr;
 }
 
+// calc_flow runs iterations 0 .. max_iter-1.  A sample whose next block
+// would pass that runs its last iterations alone on its own stream with the
+// single-problem sweeps; they hold no convergence check (the last one was at
+// the end of the previous block, and the next would be a full block away).
+pm_status run_tail(Res& r) {
+  pm_problem* pr = r.pr;
+  const int n = pr->prm.max_iter - r.it;
+  if (n <= 0) return PM_OK;
+  pr->iteration = r.it;
+  pm_status st = iterate_n(pr, n);
+  if (st == PM_OK) st = problem_flush(pr);
+  if (st == PM_OK && cudaStreamSynchronize(problem_stream(pr)) != cudaSuccess)
+    st = cuda_error(cudaGetLastError(), "final iterations");
+  r.it += n;
+  pr->sweeps_done = r.it;
+  return st;
+}
+
+// Completes a finished sample (result from its resident state) and frees it.
+void retire(pm_server* s, Res& r, pm_status st) {
+  pm_problem* pr = r.pr;
+  const pm_params& p = pr->prm;
+  pm_result out;
+  memset(&out, 0, sizeof out);
+  if (st == PM_OK) st = pm_compute_permeability(pr, &out);
+  out.iterations = r.last_check;
+  out.sweeps = r.it;
+  out.conv = r.conv;
+  out.converged = r.conv_valid && r.conv < p.eps;
+  out.permeability = r.perm;
+  if (st == PM_OK && (!isfinite(out.wk33) || !isfinite(r.perm))) st = PM_ERR_NONFINITE;
+  complete(s, r.ticket, st, st == PM_OK || st == PM_ERR_NONFINITE ? &out : nullptr, r.submit_ms,
+           r.admit_ms);
+  pm_problem_destroy(pr);
+  s->used -= r.bytes;
+}
+
 pm_status admit(pm_server* s) {
   while (!s->queue.empty() && (int)s->res.size() < s->cfg.max_resident) {
     Req& q = s->queue.front();
@@ -171,9 +208,13 @@ pm_status admit(pm_server* s) {
     r.admit_ms = now_ms(s);
     r.bytes = bytes;
     r.it = 1;
-    s->res.push_back(r);
     s->used += bytes;
     s->queue.pop_front();
+    if (r.it + s->block > p.max_iter) {  // fewer iterations than one block: alone
+      retire(s, r, run_tail(r));
+      continue;
+    }
+    s->res.push_back(r);
     s->dirty = true;
   }
   return PM_OK;
@@ -381,23 +422,12 @@ pm_status after_block(pm_server* s) {
       r.conv_valid = true;
       r.last_check = last;
     }
-    bool finished = (r.conv_valid && !(r.conv >= p.eps)) || r.it >= p.max_iter;
-    if (!finished) {
+    const bool finished = (r.conv_valid && !(r.conv >= p.eps)) || r.it >= p.max_iter;
+    if (!finished && r.it + s->block <= p.max_iter) {
       keep.push_back(r);
       continue;
     }
-    pm_result out;
-    memset(&out, 0, sizeof out);
-    pm_status st = pm_compute_permeability(pr, &out);
-    out.iterations = r.last_check;
-    out.sweeps = r.it;
-    out.conv = r.conv;
-    out.converged = r.conv_valid && r.conv < p.eps;
-    out.permeability = r.perm;
-    if (st == PM_OK && (!isfinite(out.wk33) || !isfinite(r.perm))) st = PM_ERR_NONFINITE;
-    complete(s, r.ticket, st, &out, r.submit_ms, r.admit_ms);
-    pm_problem_destroy(pr);
-    s->used -= r.bytes;
+    retire(s, r, finished ? PM_OK : run_tail(r));
     changed = true;
   }
   s->res.swap(keep);

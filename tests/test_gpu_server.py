@@ -144,3 +144,34 @@ def test_mixed_server_k_within_1e6_of_fp64():
         r64 = single(g, precision="fp64", kw=kw)
         for a in ("wk13", "wk23", "wk33"):
             assert abs(getattr(mx[i].result, a) - getattr(r64, a)) <= 1e-6 * abs(r64.wk33)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_iteration_cap_matches_single_problem(precision):
+    """Requests that stop on max_iter (eps too small to be met) run iterations
+    0 .. max_iter-1 as calc_flow does -- also when max_iter is not a block
+    boundary, or is shorter than one block -- and give the single-problem
+    result bit for bit."""
+    geoms = samples(3, seed=8)
+    caps = [1550, 250, 1301]
+    s = pm.Server(precision=precision, use_graphs=1, autotune=0)
+    tickets = {}
+    for i, (g, cap) in enumerate(zip(geoms, caps)):
+        tickets[s.submit(g, **dict(KW, eps=1e-30, max_iter=cap))] = i
+    res = {}
+    for _ in range(1000):
+        active = s.step()
+        for c in s.poll():
+            res[tickets[c.ticket]] = c
+        if active == 0 and len(res) == len(geoms):
+            break
+    s.close()
+    assert len(res) == len(geoms)
+    for i, (g, cap) in enumerate(zip(geoms, caps)):
+        r = single(g, precision=precision, kw=dict(eps=1e-30, max_iter=cap))
+        c = res[i]
+        assert c.status == 0 and not c.result.converged and not r.converged
+        assert c.result.sweeps == r.sweeps == cap
+        assert c.result.iterations == r.iterations
+        for a in ("wk13", "wk23", "wk33", "wmax_velz", "wmean_velz"):
+            assert getattr(c.result, a) == getattr(r, a), (i, a)
