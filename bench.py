@@ -434,7 +434,9 @@ def c4_samples(n: int, seed: int = 4):
 
 def c5_samples(n: int, max_axis: int, seed: int = 5):
     """Serving stream: axes log-uniform in [32, max_axis], generators as c4,
-    porosity U[0.12,0.45], boundary_method in {0,1,2}."""
+    porosity U[0.12,0.45], boundary_method in {0,1,2}.  A Gaussian draw that
+    does not percolate along z at its porosity (low porosity, large sigma,
+    long z) is redrawn with the porosity raised in steps of 0.02."""
     from poremaps_gb300 import synth
 
     rng = np.random.default_rng(seed)
@@ -448,13 +450,35 @@ def c5_samples(n: int, max_axis: int, seed: int = 5):
                                   seed=seed * 100003 + i)
         else:
             g = synth.gaussian_field(shape, float(rng.uniform(1.5, 4.0)), phi,
-                                     seed=seed * 100003 + i)
+                                     seed=seed * 100003 + i, relax=0.02)
         out.append((g, bc))
     return out
 
 
 SERVE_KW = dict(solving_algorithm=2, voxel_size=1e-5, eps=1e-6, it_eval=100, it_write=100,
                 max_iter=200000)
+# Below this |wk33| (1e-10 dx^2) a sample's permeability is numerically zero
+# (e.g. a percolating cluster whose throats are one voxel wide): the fields
+# are round-off around a zero-flow state and a relative error means nothing.
+K_ZERO = 1e-10 * SERVE_KW["voxel_size"] ** 2
+
+
+def k_errors(pairs):
+    """pairs: (mixed result, fp64 result) per sample.  Relative error of the
+    three components (over |wk33|) where k is not numerically zero; absolute
+    values listed for the rest."""
+    rel, zero = [], []
+    for i, (m, r) in enumerate(pairs):
+        d = max(abs(m.wk13 - r.wk13), abs(m.wk23 - r.wk23), abs(m.wk33 - r.wk33))
+        if abs(r.wk33) < K_ZERO:
+            zero.append({"index": i, "fp64_wk33": r.wk33, "mixed_wk33": m.wk33, "abs_diff": d})
+            rel.append(0.0)
+        else:
+            rel.append(d / abs(r.wk33))
+    nz = [x for i, x in enumerate(rel) if not any(z["index"] == i for z in zero)]
+    return rel, {"max": max(nz) if nz else 0.0, "median": float(np.median(nz)) if nz else 0.0,
+                 "samples_above_1e-6": sum(x > 1e-6 for x in nz),
+                 "numerically_zero_k": {"threshold_m2": K_ZERO, "samples": zero}}
 
 
 def run_c4(args):
@@ -486,8 +510,7 @@ def run_c4(args):
                         **SERVE_KW) as p:
             plain.append(p.solve())
     t_64 = time.perf_counter() - t0
-    rel = [max(abs(done[i].result.wk33 - r.wk33), abs(done[i].result.wk13 - r.wk13),
-               abs(done[i].result.wk23 - r.wk23)) / abs(r.wk33) for i, r in enumerate(plain)]
+    rel, kerr = k_errors([(done[i].result, r) for i, r in enumerate(plain)])
     out = {"metric": "solves/h", "value": 3600.0 * len(reqs) / t_mx, "unit": "solves/h",
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
            "config": {"workload": f"{len(reqs)} uneven samples (axes from {{32,48,64,96,128}}), "
@@ -498,14 +521,16 @@ def run_c4(args):
                              "device_busy_ms": busy, "glups_busy": lups / (busy * 1e6)},
            "plain_fp64": {"solves_per_h": 3600.0 * len(reqs) / t_64, "seconds": t_64},
            "speedup_vs_plain_fp64": t_64 / t_mx,
-           "k_rel_err_vs_plain_fp64": {"max": max(rel), "median": float(np.median(rel))},
+           "k_rel_err_vs_plain_fp64": kerr,
            "iterations": {"min": min(c.result.sweeps for c in done.values()),
                           "max": max(c.result.sweeps for c in done.values())}}
     order = sorted(range(len(rel)), key=lambda i: -rel[i])
-    out["k_rel_err_vs_plain_fp64"]["samples_above_1e-6"] = sum(r > 1e-6 for r in rel)
+    out["failed"] = [{"index": i, "status": done[i].status} for i in range(len(reqs))
+                     if done[i].status != 0]
     out["worst_samples"] = [
         {"index": i, "shape": list(reqs[i][0].shape), "boundary_method": reqs[i][1],
          "porosity": round(float(1 - reqs[i][0].mean()), 4), "rel_err": rel[i],
+         "status": done[i].status,
          "mixed": {"iterations": done[i].result.iterations,
                    "converged": bool(done[i].result.converged), "wk33": done[i].result.wk33},
          "fp64": {"iterations": plain[i].iterations, "converged": bool(plain[i].converged),
@@ -519,8 +544,8 @@ def run_c5(args):
 
     pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     reqs = c5_samples(args.samples, args.max_axis)
-    # arrival rate: keep the device busy -- mean inter-arrival = 0.8 x the mean
-    # solve time measured on the first requests alone
+    # arrival rate: keep the device busy -- mean inter-arrival = 0.6 x the mean
+    # solve time estimated from the first request alone (scaled by voxels)
     rng = np.random.default_rng(55)
     srv = pm.Server(precision="mixed", use_graphs=1, autotune=1)
     probe = time.perf_counter()
@@ -529,7 +554,7 @@ def run_c5(args):
         pass
     srv.poll()
     solo = time.perf_counter() - probe
-    gaps = rng.exponential(0.8 * solo * np.mean([g.size for g, _ in reqs]) / reqs[0][0].size,
+    gaps = rng.exponential(0.6 * solo * np.mean([g.size for g, _ in reqs]) / reqs[0][0].size,
                            len(reqs))
     arrive = np.cumsum(gaps) - gaps[0]
     t0 = time.perf_counter()
@@ -548,6 +573,24 @@ def run_c5(args):
     busy, wall, lups = srv.stats()
     srv.close()
     lat = np.array([c.finish_ms - c.submit_ms for c in done.values()]) / 1e3
+    # the plain FP64 GPU form on the same arrivals: one request at a time,
+    # first come first served; each service time is a real solve on the GPU
+    # (host geometry in, result out), the queueing follows from the arrivals
+    free_at, lat64, fp64_res, fp64_objs = 0.0, [], [], []
+    for i, (g, bc) in enumerate(reqs):
+        s0 = time.perf_counter()
+        with pm.Problem(g, None, boundary_method=bc, precision="fp64", order="jacobi",
+                        **SERVE_KW) as p:
+            r = p.solve()
+        fp64_res.append({"iterations": r.iterations, "sweeps": r.sweeps,
+                         "converged": bool(r.converged), "k": [r.wk13, r.wk23, r.wk33]})
+        svc = time.perf_counter() - s0
+        start = max(arrive[i], free_at)
+        free_at = start + svc
+        lat64.append(free_at - arrive[i])
+        fp64_objs.append(r)
+    rel, kerr = k_errors([(done[i].result, r) for i, r in enumerate(fp64_objs)])
+    lat64 = np.array(lat64)
     out = {"metric": "p99 time-to-permeability", "value": float(np.percentile(lat, 99)),
            "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f32+f64",
            "data": "synthetic",
@@ -556,7 +599,23 @@ def run_c5(args):
                                   "eps 1e-6, mixed-precision server"},
            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
            "solves_per_h": 3600.0 * len(reqs) / total,
-           "device_busy_frac": (busy / 1e3) / total}
+           "device_busy_frac": (busy / 1e3) / total,
+           "plain_fp64": {"p50_s": float(np.percentile(lat64, 50)),
+                          "p99_s": float(np.percentile(lat64, 99)),
+                          "solves_per_h": 3600.0 * len(reqs) / (free_at - arrive[0]),
+                          "service": "one request at a time, FIFO, same arrivals"},
+           "k_rel_err_vs_plain_fp64": kerr,
+           "failed": [{"index": i, "status": done[i].status} for i in range(len(reqs))
+                      if done[i].status != 0]}
+    order = sorted(range(len(rel)), key=lambda i: -rel[i])
+    out["worst_samples"] = [
+        {"index": i, "shape": list(reqs[i][0].shape), "boundary_method": reqs[i][1],
+         "porosity": round(float(1 - reqs[i][0].mean()), 4), "rel_err": rel[i],
+         "status": done[i].status,
+         "mixed": {"iterations": done[i].result.iterations, "sweeps": done[i].result.sweeps,
+                   "converged": bool(done[i].result.converged),
+                   "k": [done[i].result.wk13, done[i].result.wk23, done[i].result.wk33]},
+         "fp64": fp64_res[i]} for i in order[:4]]
     print(json.dumps(out), flush=True)
     return 0
 

@@ -85,10 +85,20 @@ def sphere_pack(shape=(128, 128, 128), rmin: float = 4.0, rmax: float = 10.0,
 
 
 def gaussian_field(shape=(64, 64, 64), sigma: float = 3.0, porosity: float = 0.2, seed: int = 0,
-                   keep_largest: bool = True, max_tries: int = 20) -> np.ndarray:
+                   keep_largest: bool = True, max_tries: int = 20,
+                   relax: float = 0.0) -> np.ndarray:
     """iid N(0,1) -> periodic Gaussian filter (sigma voxels) -> fluid = lowest
     `porosity` quantile; optionally keep only the largest z-percolating fluid
-    cluster (other pores become solid)."""
+    cluster (other pores become solid).  relax > 0: when max_tries draws do
+    not percolate, raise the porosity by relax and draw again (up to 0.6)."""
+    if relax > 0.0:
+        while True:
+            try:
+                return gaussian_field(shape, sigma, porosity, seed, keep_largest, max_tries)
+            except RuntimeError:
+                if porosity + relax > 0.6:
+                    raise
+                porosity += relax
     for attempt in range(max_tries):
         rng = np.random.default_rng(seed + 7919 * attempt)
         f = ndimage.gaussian_filter(rng.standard_normal(shape), sigma, mode="wrap")
