@@ -244,6 +244,44 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   return device_sync(pr, "kernel autotune");
 }
 
+// Block size of the reference-order wavefront, timed on the problem: a few
+// iterations on the second state buffer (a copy of the initial state, restored
+// afterwards) per candidate; every shape gives bitwise identical fields.
+// Shared across alike problems as the correction-sweep choice is.
+pm_status choose_wavefront_shape(pm_problem* pr) {
+  static std::mutex mu;
+  static std::map<std::array<long long, 5>, int> tuned;
+  std::lock_guard<std::mutex> lock(mu);
+  const std::array<long long, 5> key = {pr->g.nx, pr->g.ny, pr->g.nz, pr->solver,
+                                        pr->prm.boundary_method};
+  auto hit = tuned.find(key);
+  if (hit != tuned.end()) {
+    pr->coop_threads = hit->second;
+    pr->coop_blocks = 0;
+    return PM_OK;
+  }
+  static const int cand[] = {256, 128, 64, 32};
+  float best = 1e30f;
+  int bt = 256;
+  for (int t : cand) {
+    int blocks = 0;
+    CK(launch_wavefront(pr->F[1], pr->codes, pr->g, pr->solver, 1, t, &blocks, pr->st));
+    CK(cudaEventRecord(pr->ev0, pr->st));
+    CK(launch_wavefront(pr->F[1], pr->codes, pr->g, pr->solver, 2, t, &blocks, pr->st));
+    CK(cudaEventRecord(pr->ev1, pr->st));
+    pm_status s = device_sync(pr, "wavefront shape");
+    if (s != PM_OK) return s;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+    if (ms < 0.98f * best) { best = ms; bt = t; }
+  }
+  CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
+  pr->coop_threads = bt;
+  pr->coop_blocks = 0;
+  tuned[key] = bt;
+  return device_sync(pr, "wavefront shape");
+}
+
 pm_status dc_flush(pm_problem* pr) {
   if (pr->dc_pos > 0) {
     CK(launch_dc_correct(pr->F[pr->cur], pr->E[pr->ecur], pr->g, pr->st));
@@ -280,7 +318,8 @@ pm_status iterate_mixed(pm_problem* pr) {
 pm_status pm::iterate_n(pm_problem* pr, int n) {
   if (n <= 0) return PM_OK;
   if (pr->order == PM_ORDER_REFERENCE) {
-    CK(launch_wavefront(pr->F[pr->cur], pr->codes, pr->g, pr->solver, n, &pr->coop_blocks,
+    CK(launch_wavefront(pr->F[pr->cur], pr->codes, pr->g, pr->solver, n, pr->coop_threads,
+                        &pr->coop_blocks,
                         pr->st));
   } else {
     for (int i = 0; i < n; ++i) {
@@ -527,6 +566,10 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   }
   if (pr->precision == PM_PREC_MIXED) {
     pm_status ts = choose_correction_kernel(pr, p->kernel);
+    if (ts != PM_OK) return fail(ts);
+  }
+  if (pr->order == PM_ORDER_REFERENCE) {
+    pm_status ts = choose_wavefront_shape(pr);
     if (ts != PM_OK) return fail(ts);
   }
   unsigned long long* hc = (unsigned long long*)((char*)pr->hout + 64);

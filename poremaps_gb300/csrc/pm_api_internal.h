@@ -35,6 +35,7 @@ struct pm_problem {
   void* scratch = nullptr;  // export buffer
   size_t scratch_bytes = 0;
   int coop_blocks = 0;
+  int coop_threads = 256;  // block size of the reference-order wavefront
   pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
   pm::BrickPlan* bp = nullptr;   // TMA brick plan of the mixed form
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)

@@ -89,7 +89,8 @@ cudaError_t launch_reapply64(double* p, const uint8_t* codes, const Grid& g, cud
 // Reference order: in-place lexicographic sweep as an exact hyperplane
 // wavefront, then halo exchange and reapply, n_iter times (cooperative launch).
 cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid& g,
-                             int solver, int n_iter, int* coop_blocks, cudaStream_t st);
+                             int solver, int n_iter, int threads, int* coop_blocks,
+                             cudaStream_t st);
 
 // Ping-pong Jacobi (phase 0) and red (1) / black (2) half-sweeps from A into B
 // over the fluid list; periodic halo copies and the pressure reapply fused.

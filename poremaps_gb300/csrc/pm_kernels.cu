@@ -458,17 +458,22 @@ __global__ void __launch_bounds__(256) k_wavefront(Fields<double> f, const uint8
   }
 }
 
+// threads: block size (32..256).  The grid holds one thread per (y, z) pair
+// of a hyperplane -- enough for any hyperplane -- as far as co-residency
+// allows; smaller blocks spread the same threads over more SMs (more FP64
+// throughput per hyperplane, a dearer grid barrier).
 cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid& g, int solver,
-                             int n_iter, int* coop_blocks, cudaStream_t st) {
+                             int n_iter, int threads, int* coop_blocks, cudaStream_t st) {
   void* fn = solver == 1 ? (void*)k_wavefront<1> : solver == 2 ? (void*)k_wavefront<2>
                                                                : (void*)k_wavefront<3>;
+  if (threads < 32 || threads > 256) threads = 256;
   if (*coop_blocks <= 0) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
     if (e != cudaSuccess) return e;
-    long long want = ((long long)g.ny * g.nz + 255) / 256;  // enough for one hyperplane
+    long long want = ((long long)g.ny * g.nz + threads - 1) / threads;
     long long maxb = (long long)sms * (per > 0 ? per : 1);
     *coop_blocks = (int)(want < maxb ? (want < 1 ? 1 : want) : maxb);
   }
@@ -478,7 +483,7 @@ cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid&
   int n = n_iter;
   void* args[] = {&ff, &cc, &gg, &n};
   count_launches(1);
-  return cudaLaunchCooperativeKernel(fn, dim3(*coop_blocks), dim3(256), args, 0, st);
+  return cudaLaunchCooperativeKernel(fn, dim3(*coop_blocks), dim3(threads), args, 0, st);
 }
 
 // ------------------------------------------------------------------ FP64 sweeps (exact)
