@@ -284,7 +284,8 @@ pm_status choose_wavefront_shape(pm_problem* pr) {
 
 pm_status dc_flush(pm_problem* pr) {
   if (pr->dc_pos > 0) {
-    CK(launch_dc_correct(pr->F[pr->cur], pr->E[pr->ecur], pr->g, pr->st));
+    CK(launch_dc_correct_list(pr->F[pr->cur], pr->E[pr->ecur], pr->list, pr->nlist, pr->g,
+                              pr->st));
     pr->dc_pos = 0;
   }
   return PM_OK;
@@ -346,9 +347,14 @@ pm_status reduce_launch(pm_problem* pr, int full) {
                        pr->st));
     return PM_OK;
   }
-  CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
-                   pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
-                   pr->prm.dom_interest, pr->partials, pr->dout, pr->st));
+  if (!full) {
+    CK(launch_reduce_check(pr->F[pr->cur], pr->E[pr->ecur], mode, pr->list, pr->nlist, pr->g,
+                           pr->partials, pr->dout, pr->st));
+  } else {
+    CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
+                     pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
+                     pr->prm.dom_interest, pr->partials, pr->dout, pr->st));
+  }
   CK(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(double) * kRedVals, cudaMemcpyDeviceToHost,
                      pr->st));
   return PM_OK;

@@ -66,6 +66,25 @@ __global__ void k_dc_correct(Fields<double> x, const float4* e, Grid g) {
   }
 }
 
+// x += e over the fluid list and the periodic halo copies its sweeps write:
+// the only places where e is non-zero (residual and correction sweeps write a
+// fluid voxel and its copies), so the state equals that of the dense form
+// while solid regions are never touched.
+__global__ void k_dc_correct_list(Fields<double> x, const float4* e, const int* list, int nlist,
+                                  Grid g) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
+    dc_correct_voxel(x, e, g, __ldg(list + q));
+}
+
+cudaError_t launch_dc_correct_list(Fields<double> x, const float4* e, const int* list, int nlist,
+                                   const Grid& g, cudaStream_t st) {
+  int blocks = (nlist + 255) / 256;
+  if (blocks < 1) return cudaSuccess;
+  k_dc_correct_list<<<blocks, 256, 0, st>>>(x, e, list, nlist, g);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st) {
   k_dc_correct<<<1184, 256, 0, st>>>(x, e, g);
   count_launches(1);

@@ -101,6 +101,9 @@ cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* co
 // Mixed precision (defect correction).  x: FP64 state, e: FP32 correction
 // (ping-pong), r: FP32 residual; e and r interleaved (float4 u, v, w, p).
 cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st);
+// The same over the fluid list (and the halo copies its sweeps write).
+cudaError_t launch_dc_correct_list(Fields<double> x, const float4* e, const int* list, int nlist,
+                                   const Grid& g, cudaStream_t st);
 cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
                                const int* list, int nlist, const Grid& g, int solver,
                                cudaStream_t st);
@@ -121,6 +124,11 @@ cudaError_t launch_zero4(float4* e, const Grid& g, cudaStream_t st);
 // sums w.  partials: kRedBlocks*kRedVals doubles; out: kRedVals doubles.
 // implied3: the state stores swept pressure on the last interior plane and the
 // reapplied 3 is implied there (out-of-place orderings).
+// The convergence check's sum (value 2: sum of w, + e.z in mode 1) over the
+// fluid list; the other values of out are 0.
+cudaError_t launch_reduce_check(Fields<double> x, const float4* e, int mode, const int* list,
+                                int nlist, const Grid& g, double* partials, double* out,
+                                cudaStream_t st);
 cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
                           const uint8_t* codes, const Grid& g, const int di[6],
                           double* partials, double* out, cudaStream_t st);

@@ -573,23 +573,67 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, const 
   if (threadIdx.x < kRedVals) partials[blockIdx.x * kRedVals + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void k_reduce_final(const double* partials, double* out) {
-  // one block of 1024 threads, fixed tree over kRedBlocks partials
-  __shared__ double sh[1024];
-  for (int i = 0; i < kRedVals; ++i) {
-    double a = (threadIdx.x < (unsigned)kRedBlocks) ? partials[threadIdx.x * kRedVals + i] : 0.0;
-    sh[threadIdx.x] = a;
-    __syncthreads();
-    for (int o = 512; o > 0; o >>= 1) {
-      if (threadIdx.x < (unsigned)o) {
-        double x = sh[threadIdx.x], y = sh[threadIdx.x + o];
-        sh[threadIdx.x] = (i == 3) ? (y > x ? y : x) : x + y;
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) out[i] = sh[0];
-    __syncthreads();
+// The convergence check's sum alone (sum of w over the fluid voxels, value 2
+// of the partials; the others are 0) over the fluid list: fixed per-thread
+// order, fixed shuffle tree per warp, fixed order over the block's warps.
+template <int MODE>
+__global__ void __launch_bounds__(kRedThreads) k_reduce_check(Fields<double> x, const float4* e,
+                                                              const int* list, int nlist,
+                                                              Grid g, double* partials) {
+  double acc = 0.0;
+  for (int q = blockIdx.x * kRedThreads + threadIdx.x; q < nlist; q += kRedBlocks * kRedThreads) {
+    int X, Y, Z;
+    lin_to_xyz(__ldg(list + q), g, X, Y, Z);
+    double w = x.w[(long long)Z * g.pl64 + (long long)Y * g.px64 + X];
+    if (MODE == 1) w += (double)e[(long long)Z * g.pl4 + (long long)Y * g.px4 + X].z;
+    acc += w;
   }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sw[kRedThreads / 32];
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < kRedVals) {
+    double t = 0.0;
+    if (threadIdx.x == 2)
+      for (int w = 0; w < kRedThreads / 32; ++w) t += sw[w];
+    partials[blockIdx.x * kRedVals + threadIdx.x] = t;
+  }
+}
+
+// One warp per value: each lane folds the partials lane, lane + 32, ... in
+// order, then a fixed shuffle tree combines the lanes (deterministic).
+__global__ void __launch_bounds__(32 * kRedVals) k_reduce_final(const double* partials,
+                                                                double* out) {
+  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool is_max = i == 3;
+  constexpr int kPer = (kRedBlocks + 31) / 32;
+  double v[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {  // every load in flight at once
+    const int b = lane + 32 * k;
+    v[k] = b < kRedBlocks ? partials[b * kRedVals + i] : 0.0;
+  }
+  // the partial maxima are >= 0 (each block's starts at 0), so 0 pads them
+  double a = v[0];
+#pragma unroll
+  for (int k = 1; k < kPer; ++k) a = is_max ? (v[k] > a ? v[k] : a) : a + v[k];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double y = __shfl_xor_sync(0xffffffffu, a, o);
+    a = is_max ? (y > a ? y : a) : a + y;
+  }
+  if (lane == 0) out[i] = a;
+}
+
+cudaError_t launch_reduce_check(Fields<double> x, const float4* e, int mode, const int* list,
+                                int nlist, const Grid& g, double* partials, double* out,
+                                cudaStream_t st) {
+  if (mode == 0)
+    k_reduce_check<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, list, nlist, g, partials);
+  else
+    k_reduce_check<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, list, nlist, g, partials);
+  k_reduce_final<<<1, 32 * kRedVals, 0, st>>>(partials, out);
+  count_launches(2);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
@@ -601,7 +645,7 @@ cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full,
   else
     k_reduce<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
                                                      di[2], di[3], di[4], di[5], partials);
-  k_reduce_final<<<1, 1024, 0, st>>>(partials, out);
+  k_reduce_final<<<1, 32 * kRedVals, 0, st>>>(partials, out);
   count_launches(2);
   return cudaGetLastError();
 }
