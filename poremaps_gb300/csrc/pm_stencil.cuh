@@ -304,31 +304,16 @@ __device__ __forceinline__ void sweep64_voxel(const Fields<double>& A, const Fie
 // The stencil of one voxel from the correction: the union of its offsets is
 // 13 points, each one 128-bit load.  The voxel's own pressure on the last
 // interior plane is the reapplied (fixed) value, whose correction is 0.
-// The values two voxels away along an axis enter the update only for wall
-// cases 4 (second right) and 5 (second left) of that axis (case_pick): for
-// the other cases they are not loaded at all (their stencil entries stay 0
-// and are never read), which spares up to 6 of the 13 loads per voxel.
-constexpr bool kFarOnDemand = true;
-
 __device__ __forceinline__ void gather4(Stencil<float>& s, const float4* E, long long c, int z,
-                                        const Grid& g, int code) {
+                                        const Grid& g) {
   const long long px = g.px4, pl = g.pl4;
-  bool xmm = true, xpp = true, ymm = true, ypp = true, zmm = true, zpp = true;
-  if (kFarOnDemand) {
-    int cx, cy, cz;
-    decode_cases(code, cx, cy, cz);
-    xmm = cx == 5; xpp = cx == 4; ymm = cy == 5; ypp = cy == 4; zmm = cz == 5; zpp = cz == 4;
-  }
-  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 C = __ldg(E + c);
   const float4 XM = __ldg(E + c - 1), XP = __ldg(E + c + 1);
-  const float4 XMM = xmm ? __ldg(E + c - 2) : zero, XPP = xpp ? __ldg(E + c + 2) : zero;
+  const float4 XMM = __ldg(E + c - 2), XPP = __ldg(E + c + 2);
   const float4 YM = __ldg(E + c - px), YP = __ldg(E + c + px);
-  const float4 YMM = ymm ? __ldg(E + c - 2 * px) : zero;
-  const float4 YPP = ypp ? __ldg(E + c + 2 * px) : zero;
+  const float4 YMM = __ldg(E + c - 2 * px), YPP = __ldg(E + c + 2 * px);
   const float4 ZM = __ldg(E + c - pl), ZP = __ldg(E + c + pl);
-  const float4 ZMM = zmm ? __ldg(E + c - 2 * pl) : zero;
-  const float4 ZPP = zpp ? __ldg(E + c + 2 * pl) : zero;
+  const float4 ZMM = __ldg(E + c - 2 * pl), ZPP = __ldg(E + c + 2 * pl);
   s.uc = C.x; s.uxm = XM.x; s.uxp = XP.x; s.uym = YM.x; s.uyp = YP.x;
   s.uymm = YMM.x; s.uypp = YPP.x; s.uzm = ZM.x; s.uzp = ZP.x; s.uzmm = ZMM.x; s.uzpp = ZPP.x;
   s.vc = C.y; s.vxm = XM.y; s.vxp = XP.y; s.vxmm = XMM.y; s.vxpp = XPP.y; s.vym = YM.y;
@@ -393,7 +378,7 @@ __device__ __forceinline__ void dc_inner_voxel(const float4* E, float4* E2, cons
   int code = codes[((long long)z * g.NY + y) * g.pxc + x];
   long long c = (long long)z * g.pl4 + (long long)y * g.px4 + x;
   Stencil<float> s;
-  gather4(s, E, c, z, g, code);
+  gather4(s, E, c, z, g);
   float un, vn, wn, pn;
   update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
   const float4 r = __ldg(R + c);
