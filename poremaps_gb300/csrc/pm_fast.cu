@@ -27,15 +27,48 @@ cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* cod
                           const int* list, int nlist, const Grid& g, int solver, int phase,
                           cudaStream_t st);
 
+// Persistent form: one wave of two CTAs per SM walks the list with a grid
+// stride, each thread loading its next list entry before it computes the
+// current voxel (the FP64 stencil needs ~110 registers: two CTAs fit).
+template <int SOLVER, int PHASE>
+__global__ void __launch_bounds__(256, 2) k_sweep64_pf(Fields<double> A, Fields<double> B,
+                                                      const uint8_t* codes, const int* list,
+                                                      int nlist, Grid g) {
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  int lin = q < nlist ? __ldg(list + q) : 0;
+  for (; q < nlist; q += stride) {
+    const int qn = q + stride;
+    const int next = qn < nlist ? __ldg(list + qn) : 0;
+    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, lin);
+    lin = next;
+  }
+}
+
+constexpr bool kSweep64Persistent = true;
+
 template <int SOLVER>
 static cudaError_t sweep_fast_s(Fields<double> A, Fields<double> B, const uint8_t* codes,
                                 const int* list, int nlist, const Grid& g, int phase,
                                 cudaStream_t st) {
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
-  if (phase == 0) k_sweep64_fast<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
-  else if (phase == 1) k_sweep64_fast<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
-  else k_sweep64_fast<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  if (kSweep64Persistent) {
+    static int sms = 0;
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (blocks > 2 * sms) blocks = 2 * sms;
+    if (phase == 0) k_sweep64_pf<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+    else if (phase == 1) k_sweep64_pf<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+    else k_sweep64_pf<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  } else {
+    if (phase == 0) k_sweep64_fast<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+    else if (phase == 1) k_sweep64_fast<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+    else k_sweep64_fast<SOLVER, 2><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
@@ -93,18 +126,33 @@ cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, 
 
 // r = F(x) - x in FP64 (stored FP32) and the first correction e1 = r.
 template <int SOLVER>
-__global__ void __launch_bounds__(256) k_dc_residual(Fields<double> X, float4* R, float4* E,
-                                                     const uint8_t* codes, const int* list,
-                                                     int nlist, Grid g) {
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
-    dc_residual_voxel<SOLVER>(X, R, E, codes, g, list[q]);
+__global__ void __launch_bounds__(256, 2) k_dc_residual(Fields<double> X, float4* R, float4* E,
+                                                      const uint8_t* codes, const int* list,
+                                                      int nlist, Grid g) {
+  // persistent, next list entry prefetched (as the FP64 sweeps)
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  int lin = q < nlist ? __ldg(list + q) : 0;
+  for (; q < nlist; q += stride) {
+    const int qn = q + stride;
+    const int next = qn < nlist ? __ldg(list + qn) : 0;
+    dc_residual_voxel<SOLVER>(X, R, E, codes, g, lin);
+    lin = next;
+  }
 }
 
 cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
                                const int* list, int nlist, const Grid& g, int solver,
                                cudaStream_t st) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
+  if (blocks > 2 * sms) blocks = 2 * sms;
   if (solver == 1) k_dc_residual<1><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
   else if (solver == 2) k_dc_residual<2><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
   else k_dc_residual<3><<<blocks, 256, 0, st>>>(x, r, e, codes, list, nlist, g);
