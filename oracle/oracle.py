@@ -64,6 +64,10 @@ def lib():
         L.or_get_nhood.argtypes = [C.c_void_p, C.c_void_p]
         L.or_get_padded.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 4
         L.or_threads.argtypes = [C.c_void_p, C.c_int]
+        L.or_set_fields.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.or_second_derivative.restype = C.c_double
+        L.or_second_derivative.argtypes = [C.c_int] + [C.c_double] * 5
+        L.or_split_code.argtypes = [C.c_int, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -128,6 +132,11 @@ class OracleProblem:
         lib().or_get_fields(self.h, *[a.ctypes.data for a in arr])
         return Fields(*arr)
 
+    def set_fields(self, u=None, v=None, w=None, p=None) -> None:
+        """Interior fields (z, y, x) set directly (test hook)."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (u, v, w, p)]
+        lib().or_set_fields(self.h, *[None if a is None else a.ctypes.data for a in arrs])
+
     def nhood(self) -> np.ndarray:
         out = np.empty(self.shape, np.int32)
         lib().or_get_nhood(self.h, out.ctypes.data)
@@ -149,3 +158,15 @@ def run_reference_binary(inp_path: str, cwd: str, nranks: int = 1, timeout: floa
     env = dict(os.environ, PM_SHIM_NP=str(nranks))
     return subprocess.run([REF_BIN, inp_path], cwd=cwd, env=env, capture_output=True,
                           text=True, timeout=timeout)
+
+
+def second_derivative(case: int, ll: float, l: float, m: float, r: float, rr: float) -> float:
+    """get_2nd_derivation (solver.cc:57-91) of the restatement."""
+    return lib().or_second_derivative(case, ll, l, m, r, rr)
+
+
+def split_code(code: int):
+    """split_number (solver.cc:94-109) of the restatement: (cx, cy, cz)."""
+    out = (C.c_int * 3)()
+    lib().or_split_code(code, out)
+    return tuple(out)

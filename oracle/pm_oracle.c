@@ -615,6 +615,39 @@ void or_get_fields(const or_problem* pr, double* u, double* v, double* w, double
   }
 }
 
+/* Test hooks: interior fields set directly (the evaluation routines on
+ * prescribed velocities, as the reference's tests/test_evaluation.py does),
+ * and the stencil helpers on their own (tests/test_solver.py). */
+void or_set_fields(or_problem* pr, const double* u, const double* v, const double* w,
+                   const double* p) {
+  for (int c = 0; c < pr->ns; ++c) {
+    slab* S = &pr->s[c];
+    for (int i = 0; i < S->lnz; ++i)
+      for (int j = 0; j < pr->ny; ++j)
+        for (int k = 0; k < pr->nx; ++k) {
+          long o = ((long)(S->z0 + i) * pr->ny + j) * pr->nx + k;
+          long q = IDX(S, i + 2, j + 2, k + 2);
+          if (u) S->u[q] = u[o];
+          if (v) S->v[q] = v[o];
+          if (w) S->w[q] = w[o];
+          if (p) S->p[q] = p[o];
+        }
+  }
+}
+
+double or_second_derivative(int cs, double ll, double l, double m, double r, double rr) {
+  return d2(cs, ll, l, m, r, rr);
+}
+
+void or_split_code(int code, int out[3]) {
+  /* split_number (solver.cc:94-109): 100 cx + 10 cy + cz */
+  out[2] = code % 10;
+  code /= 10;
+  out[1] = code % 10;
+  code /= 10;
+  out[0] = code % 10;
+}
+
 void or_get_nhood(const or_problem* pr, int* out) {
   for (int c = 0; c < pr->ns; ++c) {
     const slab* S = &pr->s[c];

@@ -55,6 +55,11 @@ double or_porosity(or_problem* pr);
 void or_get_fields(const or_problem* pr, double* u, double* v, double* w, double* p);
 /* Interior neighbourhood codes (100cx+10cy+cz, -1 solid), x fastest. */
 void or_get_nhood(const or_problem* pr, int* out);
+/* Test hooks: set interior fields; the stencil helpers on their own. */
+void or_set_fields(or_problem* pr, const double* u, const double* v, const double* w,
+                   const double* p);
+double or_second_derivative(int cs, double ll, double l, double m, double r, double rr);
+void or_split_code(int code, int out[3]);
 /* Full padded arrays of slab s (for halo checks). */
 void or_get_padded(const or_problem* pr, int s, int dims_out[3], double* u, double* v, double* w,
                    double* p);
