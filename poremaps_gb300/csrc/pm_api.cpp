@@ -11,6 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <map>
@@ -316,23 +317,83 @@ pm_status iterate_mixed(pm_problem* pr) {
 
 }  // namespace
 
+namespace {
+
+pm_status iterate_direct(pm_problem* pr, int n) {
+  for (int i = 0; i < n; ++i) {
+    pm_status s = pr->precision == PM_PREC_MIXED ? iterate_mixed(pr) : iterate64(pr);
+    if (s != PM_OK) return s;
+    pr->iteration++;
+    pr->sweeps_done++;
+  }
+  return PM_OK;
+}
+
+constexpr int kGraphMinSweeps = 16;  // shorter blocks are launched directly
+constexpr size_t kGraphCache = 8;
+
+}  // namespace
+
+// A block of n sweeps of the out-of-place orders runs as one CUDA graph: the
+// first time a (length, parity state) occurs the launches are captured while
+// the host bookkeeping advances as usual, later blocks with the same start
+// state replay the graph and apply the recorded end state.  Graph launches
+// cut the per-kernel launch cost that dominates small domains.
 pm_status pm::iterate_n(pm_problem* pr, int n) {
   if (n <= 0) return PM_OK;
   if (pr->order == PM_ORDER_REFERENCE) {
     CK(launch_wavefront(pr->F[pr->cur], pr->codes, pr->g, pr->solver, n, pr->coop_threads,
                         &pr->coop_blocks,
                         pr->st));
-  } else {
-    for (int i = 0; i < n; ++i) {
-      pm_status s = pr->precision == PM_PREC_MIXED ? iterate_mixed(pr) : iterate64(pr);
-      if (s != PM_OK) return s;
-      pr->iteration++;
-      pr->sweeps_done++;
-    }
+    pr->iteration += n;
+    pr->sweeps_done += n;
     return PM_OK;
   }
-  pr->iteration += n;
-  pr->sweeps_done += n;
+  // long runs go as it_eval-long chunks, whose graphs repeat
+  const int chunk = std::max(kGraphMinSweeps, pr->prm.it_eval);
+  while (n > chunk) {
+    pm_status s = iterate_n(pr, chunk);
+    if (s != PM_OK) return s;
+    n -= chunk;
+  }
+  if (n < kGraphMinSweeps) return iterate_direct(pr, n);
+  const int phase = pr->precision == PM_PREC_MIXED ? pr->iteration % pr->mixed_inner : 0;
+  for (const auto& b : pr->graphs) {
+    if (b.n == n && b.cur == pr->cur && b.ecur == pr->ecur && b.dc_pos == pr->dc_pos &&
+        b.phase == phase) {
+      CK(cudaGraphLaunch(b.exec, pr->st));
+      count_launches(b.launches);
+      pr->cur = b.cur1;
+      pr->ecur = b.ecur1;
+      pr->dc_pos = b.dc_pos1;
+      pr->iteration += n;
+      pr->sweeps_done += n;
+      return PM_OK;
+    }
+  }
+  pm_problem::BlockGraph b;
+  b.n = n; b.cur = pr->cur; b.ecur = pr->ecur; b.dc_pos = pr->dc_pos; b.phase = phase;
+  const unsigned long long l0 = launches_total();
+  CK(cudaStreamBeginCapture(pr->st, cudaStreamCaptureModeThreadLocal));
+  pm_status s = iterate_direct(pr, n);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(pr->st, &graph);
+  if (s != PM_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return s;
+  }
+  if (e != cudaSuccess) return cuda_error(e, "sweep block capture");
+  e = cudaGraphInstantiate(&b.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_error(e, "sweep block graph");
+  b.launches = launches_total() - l0;  // counted once by the capture: this launch
+  b.cur1 = pr->cur; b.ecur1 = pr->ecur; b.dc_pos1 = pr->dc_pos;
+  CK(cudaGraphLaunch(b.exec, pr->st));
+  if (pr->graphs.size() >= kGraphCache) {
+    cudaGraphExecDestroy(pr->graphs.front().exec);
+    pr->graphs.erase(pr->graphs.begin());
+  }
+  pr->graphs.push_back(b);
   return PM_OK;
 }
 
@@ -519,6 +580,7 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
     if ((e = (expr)) != cudaSuccess) return fail(cuda_error(e, #expr)); \
   } while (0)
   CKF(cudaStreamCreateWithFlags(&pr->st, cudaStreamNonBlocking));
+  sm_count();  // device query outside any later graph capture
   CKF(cudaEventCreate(&pr->ev0));
   CKF(cudaEventCreate(&pr->ev1));
   CKF(cudaMalloc((void**)&pr->codes_base, g.allocc));
@@ -595,6 +657,7 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
 pm_status pm_problem_destroy(pm_problem* pr) {
   if (!pr) return PM_OK;
   if (pr->st) cudaStreamSynchronize(pr->st);
+  for (auto& b : pr->graphs) cudaGraphExecDestroy(b.exec);
   zmarch_destroy(pr->zp);
   brick_destroy(pr->bp);
   cudaFree(pr->codes_base);

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/poremaps.h"
 #include "pm_internal.h"
 #include "pm_brick.h"
@@ -54,6 +56,16 @@ struct pm_problem {
   double phi = 0.0;
   double device_ms = 0.0;
   long long sweeps_done = 0;
+  // CUDA graphs of sweep blocks, keyed by the block length and the state
+  // parities at its start (the kernel sequence and its pointers depend on
+  // nothing else); each records the parities it ends with.
+  struct BlockGraph {
+    int n, cur, ecur, dc_pos, phase;  // phase: iteration % mixed_inner at the start
+    int cur1, ecur1, dc_pos1;
+    unsigned long long launches;
+    cudaGraphExec_t exec;
+  };
+  std::vector<BlockGraph> graphs;
 };
 
 namespace pm {

@@ -54,12 +54,7 @@ static cudaError_t sweep_fast_s(Fields<double> A, Fields<double> B, const uint8_
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
   if (kSweep64Persistent) {
-    static int sms = 0;
-    if (!sms) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = sm_count();
     if (blocks > 2 * sms) blocks = 2 * sms;
     if (phase == 0) k_sweep64_pf<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
     else if (phase == 1) k_sweep64_pf<SOLVER, 1><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
@@ -83,22 +78,6 @@ cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* co
 }
 
 // ------------------------------------------------------------------ mixed precision
-// x += e over the whole padded state (e is zero wherever no sweep writes).
-__global__ void k_dc_correct(Fields<double> x, const float4* e, Grid g) {
-  long long n = (long long)g.NX * g.NY * g.NZ;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x) {
-    int X = (int)(q % g.NX);
-    long long r = q / g.NX;
-    long long c64 = r * g.px64 + X, c4 = r * g.px4 + X;
-    const float4 v = e[c4];
-    x.u[c64] += (double)v.x;
-    x.v[c64] += (double)v.y;
-    x.w[c64] += (double)v.z;
-    x.p[c64] += (double)v.w;
-  }
-}
-
 // x += e over the fluid list and the periodic halo copies its sweeps write:
 // the only places where e is non-zero (residual and correction sweeps write a
 // fluid voxel and its copies), so the state equals that of the dense form
@@ -118,11 +97,6 @@ cudaError_t launch_dc_correct_list(Fields<double> x, const float4* e, const int*
   return cudaGetLastError();
 }
 
-cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st) {
-  k_dc_correct<<<1184, 256, 0, st>>>(x, e, g);
-  count_launches(1);
-  return cudaGetLastError();
-}
 
 // r = F(x) - x in FP64 (stored FP32) and the first correction e1 = r.
 template <int SOLVER>
@@ -144,12 +118,7 @@ __global__ void __launch_bounds__(256, 2) k_dc_residual(Fields<double> X, float4
 cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
                                const int* list, int nlist, const Grid& g, int solver,
                                cudaStream_t st) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
+  const int sms = sm_count();
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
   if (blocks > 2 * sms) blocks = 2 * sms;
@@ -205,12 +174,7 @@ template <int MINB>
 static cudaError_t launch_pf(const float4* e, float4* e2, const float4* r, const uint8_t* codes,
                              const int* list, int nlist, const Grid& g, int solver,
                              cudaStream_t st) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
+  const int sms = sm_count();
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
   if (blocks > MINB * sms) blocks = MINB * sms;

@@ -66,6 +66,9 @@ struct Counts {
 
 // Kernel launch counter (all launch wrappers add the kernels they start).
 void count_launches(int n);
+// Multiprocessors of the current device (queried once; problem creation
+// calls it first, so no launcher queries the device inside a graph capture).
+int sm_count();
 unsigned long long launches_total();
 
 // ---------------------------------------------------------------- launchers
@@ -100,8 +103,8 @@ cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* co
 
 // Mixed precision (defect correction).  x: FP64 state, e: FP32 correction
 // (ping-pong), r: FP32 residual; e and r interleaved (float4 u, v, w, p).
-cudaError_t launch_dc_correct(Fields<double> x, const float4* e, const Grid& g, cudaStream_t st);
-// The same over the fluid list (and the halo copies its sweeps write).
+// x += e over the fluid list and the halo copies its sweeps write (the only
+// places where e is non-zero).
 cudaError_t launch_dc_correct_list(Fields<double> x, const float4* e, const int* list, int nlist,
                                    const Grid& g, cudaStream_t st);
 cudaError_t launch_dc_residual(Fields<double> x, float4* r, float4* e, const uint8_t* codes,

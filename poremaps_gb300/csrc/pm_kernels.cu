@@ -18,6 +18,18 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 unsigned long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 
+int sm_count() {
+  static std::atomic<int> sms{0};
+  int v = sms.load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  if (v <= 0) v = 1;
+  sms.store(v, std::memory_order_relaxed);
+  return v;
+}
+
 Grid make_grid(int nx, int ny, int nz, int bm) {
   Grid g;
   g.nx = nx; g.ny = ny; g.nz = nz;

@@ -225,13 +225,7 @@ pm_status admit(pm_server* s) {
 // batch) the device still gets a full grid.
 void build_items(pm_server* s, int chunk) {
   s->h_items.clear();
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = sm_count();
   long long total = 0;
   for (auto& r : s->res) total += r.pr->nlist;
   const long long fill = (total + 8LL * sms - 1) / (8LL * sms);

@@ -59,6 +59,18 @@ def test_cli_default_order_converges_to_reference_k(tmp_path):
     assert abs(float(last[-1]) - float(ref[-1])) <= 2e-6 * abs(float(ref[-1]))
 
 
+def test_cli_mixed_precision_converges_to_reference_k(tmp_path):
+    """poremaps_gpu --precision mixed (FP32 sweeps + FP64 defect correction)
+    on the converged sphere case: the final permeability agrees with the
+    reference program's log to its 7 digits."""
+    log = run_cli("spheres_converged", tmp_path, ["--precision", "mixed"])
+    last = [c.strip() for c in log.strip().splitlines()[-1].split(",")]
+    ref = [c.strip() for c in str(GOLDEN["spheres_converged/log"]).strip().splitlines()[-1].split(",")]
+    assert abs(float(last[-1]) - float(ref[-1])) <= 2e-6 * abs(float(ref[-1]))
+    for pre in ("velz_", "press_"):
+        assert (tmp_path / (pre + "geom.raw")).stat().st_size == 8 * 20 * 20 * 20
+
+
 def test_c1_cylinder_full_calc_flow_reference_order():
     """48x48x64 cylinder r=20, GS, eps 1e-6: the reference stops at iteration
     64,200 with wk33 = 1.070459e-08 m^2 (Hagen-Poiseuille 1.0908e-08)."""
