@@ -138,15 +138,62 @@ pm_status iterate64(pm_problem* pr) {
   Fields<double> A = pr->F[pr->cur], B = pr->F[1 - pr->cur];
   if (pr->order == PM_ORDER_JACOBI) {
     CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
-                      pr->st));
+                      pr->st, pr->pf64[0]));
   } else {
     CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nred, pr->g, pr->solver, pr->exact, 1,
-                      pr->st));
+                      pr->st, pr->pf64[1]));
     CK(launch_sweep64(A, B, pr->codes, pr->list + pr->nred, pr->nlist - pr->nred, pr->g,
-                      pr->solver, pr->exact, 2, pr->st));
+                      pr->solver, pr->exact, 2, pr->st, pr->pf64[2]));
   }
   pr->cur = 1 - pr->cur;
   return PM_OK;
+}
+
+// Launch form of each FP64 phase (persistent or one voxel per thread), timed
+// on the problem: the persistent form wins on porous media at 128^3, the
+// one-voxel form can win where a phase needs more registers than the
+// persistent launch allows.  Both give identical fields; the trials sweep
+// the initial state into the second buffer, which is restored afterwards.
+pm_status choose_fp64_shapes(pm_problem* pr) {
+  if (pr->exact) return PM_OK;
+  static std::mutex mu;
+  static std::map<std::array<long long, 7>, std::array<int, 3>> tuned;
+  std::lock_guard<std::mutex> lock(mu);
+  const std::array<long long, 7> key = {
+      pr->g.nx, pr->g.ny, pr->g.nz, pr->solver, pr->prm.boundary_method, pr->order,
+      (long long)llround(20.0 * (double)pr->nlist / (double)pr->g.nvox)};
+  auto hit = tuned.find(key);
+  if (hit != tuned.end()) {
+    for (int i = 0; i < 3; ++i) pr->pf64[i] = hit->second[i];
+    return PM_OK;
+  }
+  const Fields<double> A = pr->F[0], B = pr->F[1];
+  const int phases[2] = {pr->order == PM_ORDER_JACOBI ? 0 : 1, 2};
+  const int nph = pr->order == PM_ORDER_JACOBI ? 1 : 2;
+  for (int k = 0; k < nph; ++k) {
+    const int ph = phases[k];
+    const int* list = ph == 2 ? pr->list + pr->nred : pr->list;
+    const int n = ph == 0 ? pr->nlist : ph == 1 ? pr->nred : pr->nlist - pr->nred;
+    float t[2] = {1e30f, 1e30f};
+    for (int form = 1; form >= 0; --form) {
+      CK(launch_sweep64(A, B, pr->codes, list, n, pr->g, pr->solver, 0, ph, pr->st, form));
+      for (int trial = 0; trial < 3; ++trial) {
+        CK(cudaEventRecord(pr->ev0, pr->st));
+        for (int r = 0; r < 3; ++r)
+          CK(launch_sweep64(A, B, pr->codes, list, n, pr->g, pr->solver, 0, ph, pr->st, form));
+        CK(cudaEventRecord(pr->ev1, pr->st));
+        pm_status s = device_sync(pr, "FP64 sweep shape");
+        if (s != PM_OK) return s;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, pr->ev0, pr->ev1));
+        if (ms < t[form]) t[form] = ms;
+      }
+    }
+    pr->pf64[ph] = t[0] < 0.98f * t[1] ? 0 : 1;
+  }
+  CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
+  tuned[key] = {pr->pf64[0], pr->pf64[1], pr->pf64[2]};
+  return device_sync(pr, "FP64 sweep shape");
 }
 
 // Correction-sweep kernels of the mixed form: 0 TMA z-march with 32 x 16
@@ -639,6 +686,9 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   if (pr->order == PM_ORDER_REFERENCE) {
     pm_status ts = choose_wavefront_shape(pr);
     if (ts != PM_OK) return fail(ts);
+  } else if (pr->precision == PM_PREC_FP64) {
+    pm_status ts = choose_fp64_shapes(pr);
+    if (ts != PM_OK) return fail(ts);
   }
   unsigned long long* hc = (unsigned long long*)((char*)pr->hout + 64);
   pr->counts = {(long long)hc[0], (long long)hc[1], (long long)hc[2], (long long)hc[3]};
@@ -857,12 +907,12 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
       Fields<double> A = pr->F[pr->cur], B = pr->F[1 - pr->cur];
       if (pr->order == PM_ORDER_JACOBI) {
         CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nlist, pr->g, pr->solver, pr->exact, 0,
-                          pr->st));
+                          pr->st, pr->pf64[0]));
       } else {
         CK(launch_sweep64(A, B, pr->codes, pr->list, pr->nred, pr->g, pr->solver, pr->exact, 1,
-                          pr->st));
+                          pr->st, pr->pf64[1]));
         CK(launch_sweep64(A, B, pr->codes, pr->list + pr->nred, pr->nlist - pr->nred, pr->g,
-                          pr->solver, pr->exact, 2, pr->st));
+                          pr->solver, pr->exact, 2, pr->st, pr->pf64[2]));
       }
     }
   }

@@ -25,7 +25,8 @@ struct pm_problem {
   uint8_t* codes = nullptr;
   int* list = nullptr;
   int nlist = 0;
-  int nred = 0;  // red-black order: the list holds the red voxels first, then black
+  int nred = 0;
+  int pf64[3] = {1, 1, 1};  // per FP64 phase (Jacobi, red, black): persistent sweep  // red-black order: the list holds the red voxels first, then black
   double* f64_base[2] = {nullptr, nullptr};
   pm::Fields<double> F[2];
   float4* f32_base = nullptr;  // e0, e1, r (interleaved u, v, w, p)

@@ -45,15 +45,13 @@ __global__ void __launch_bounds__(256, 2) k_sweep64_pf(Fields<double> A, Fields<
   }
 }
 
-constexpr bool kSweep64Persistent = true;
-
 template <int SOLVER>
 static cudaError_t sweep_fast_s(Fields<double> A, Fields<double> B, const uint8_t* codes,
                                 const int* list, int nlist, const Grid& g, int phase,
-                                cudaStream_t st) {
+                                int persistent, cudaStream_t st) {
   int blocks = (nlist + 255) / 256;
   if (blocks < 1) return cudaSuccess;
-  if (kSweep64Persistent) {
+  if (persistent) {
     const int sms = sm_count();
     if (blocks > 2 * sms) blocks = 2 * sms;
     if (phase == 0) k_sweep64_pf<SOLVER, 0><<<blocks, 256, 0, st>>>(A, B, codes, list, nlist, g);
@@ -70,11 +68,11 @@ static cudaError_t sweep_fast_s(Fields<double> A, Fields<double> B, const uint8_
 
 cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* codes,
                            const int* list, int nlist, const Grid& g, int solver, int exact,
-                           int phase, cudaStream_t st) {
+                           int phase, cudaStream_t st, int persistent) {
   if (exact) return sweep64_exact(A, B, codes, list, nlist, g, solver, phase, st);
-  if (solver == 1) return sweep_fast_s<1>(A, B, codes, list, nlist, g, phase, st);
-  if (solver == 2) return sweep_fast_s<2>(A, B, codes, list, nlist, g, phase, st);
-  return sweep_fast_s<3>(A, B, codes, list, nlist, g, phase, st);
+  if (solver == 1) return sweep_fast_s<1>(A, B, codes, list, nlist, g, phase, persistent, st);
+  if (solver == 2) return sweep_fast_s<2>(A, B, codes, list, nlist, g, phase, persistent, st);
+  return sweep_fast_s<3>(A, B, codes, list, nlist, g, phase, persistent, st);
 }
 
 // ------------------------------------------------------------------ mixed precision

@@ -97,9 +97,11 @@ cudaError_t launch_wavefront(Fields<double> f, const uint8_t* codes, const Grid&
 
 // Ping-pong Jacobi (phase 0) and red (1) / black (2) half-sweeps from A into B
 // over the fluid list; periodic halo copies and the pressure reapply fused.
+// persistent: one wave of 2 CTAs per SM walking the list (else one voxel per
+// thread); both give identical fields.
 cudaError_t launch_sweep64(Fields<double> A, Fields<double> B, const uint8_t* codes,
                            const int* list, int nlist, const Grid& g, int solver, int exact,
-                           int phase, cudaStream_t st);
+                           int phase, cudaStream_t st, int persistent = 1);
 
 // Mixed precision (defect correction).  x: FP64 state, e: FP32 correction
 // (ping-pong), r: FP32 residual; e and r interleaved (float4 u, v, w, p).
