@@ -175,3 +175,30 @@ def test_iteration_cap_matches_single_problem(precision):
         assert c.result.iterations == r.iterations
         for a in ("wk13", "wk23", "wk33", "wmax_velz", "wmean_velz"):
             assert getattr(c.result, a) == getattr(r, a), (i, a)
+
+
+def test_mixed_solvers_in_one_batch():
+    """Requests with different update formulas (GS and SOR) share the batched
+    launches through the generic kernels; each result equals its
+    single-problem run bit for bit."""
+    geoms = samples(4, seed=9)
+    solvers = [2, 3, 3, 2]
+    s = pm.Server(precision="mixed", use_graphs=1, autotune=0)
+    tickets = {}
+    for i, (g, sv) in enumerate(zip(geoms, solvers)):
+        tickets[s.submit(g, **dict(KW, solving_algorithm=sv))] = i
+    res = {}
+    for _ in range(5000):
+        active = s.step()
+        for c in s.poll():
+            res[tickets[c.ticket]] = c
+        if active == 0 and len(res) == len(geoms):
+            break
+    s.close()
+    assert len(res) == len(geoms)
+    for i, (g, sv) in enumerate(zip(geoms, solvers)):
+        r = single(g, kw=dict(solving_algorithm=sv))
+        c = res[i]
+        assert c.status == 0 and c.result.iterations == r.iterations
+        for a in ("wk13", "wk23", "wk33"):
+            assert getattr(c.result, a) == getattr(r, a), (i, a)
