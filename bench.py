@@ -408,6 +408,11 @@ def run_profile_case(args):
             p.block_timed(SWEEPS_PER_BLOCK, True)
         if args.profile_case == "mixed":
             print(json.dumps({"kernel": KERNELS[p.kernel()][0], "brick": p.brick()}), flush=True)
+    if args.profile_case == "fp64":  # and the red-black FP64 form (the default order)
+        with pm.Problem(rots[2], None, precision="fp64", solving_algorithm=3, boundary_method=0,
+                        voxel_size=1e-5, order="redblack") as p:
+            for _ in range(2):
+                p.block_timed(SWEEPS_PER_BLOCK, True)
     return 0
 
 
