@@ -5,7 +5,7 @@
 //     units that use it are compiled with -fmad=false), bit-identical to the
 //     reference CPU program;
 //   * update_fast: the same linear map regrouped into a coefficient form with
-//     FMAs (about 33 floating-point instructions per fluid voxel instead of
+//     FMAs (about 39 floating-point instructions per fluid voxel instead of
 //     ~70 plus three divisions), used by the FP64 fast sweeps and by the FP32
 //     correction sweeps of the mixed-precision form.
 #pragma once
