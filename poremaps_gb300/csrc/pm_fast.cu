@@ -19,8 +19,11 @@ template <int SOLVER, int PHASE>
 __global__ void __launch_bounds__(256) k_sweep64_fast(Fields<double> A, Fields<double> B,
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
+  __shared__ double ctab[16];
+  fill_centre_table(ctab);
+  __syncthreads();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
-    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, list[q]);
+    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, list[q], ctab);
 }
 
 cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* codes,
@@ -34,13 +37,16 @@ template <int SOLVER, int PHASE>
 __global__ void __launch_bounds__(256, 2) k_sweep64_pf(Fields<double> A, Fields<double> B,
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
+  __shared__ double ctab[16];
+  fill_centre_table(ctab);
+  __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   int lin = q < nlist ? __ldg(list + q) : 0;
   for (; q < nlist; q += stride) {
     const int qn = q + stride;
     const int next = qn < nlist ? __ldg(list + qn) : 0;
-    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, lin);
+    sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, lin, ctab);
     lin = next;
   }
 }
@@ -102,13 +108,16 @@ __global__ void __launch_bounds__(256, 2) k_dc_residual(Fields<double> X, float4
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
   // persistent, next list entry prefetched (as the FP64 sweeps)
+  __shared__ double ctab[16];
+  fill_centre_table(ctab);
+  __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   int lin = q < nlist ? __ldg(list + q) : 0;
   for (; q < nlist; q += stride) {
     const int qn = q + stride;
     const int next = qn < nlist ? __ldg(list + qn) : 0;
-    dc_residual_voxel<SOLVER>(X, R, E, codes, g, lin);
+    dc_residual_voxel<SOLVER>(X, R, E, codes, g, lin, ctab);
     lin = next;
   }
 }

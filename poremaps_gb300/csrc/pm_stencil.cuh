@@ -131,9 +131,29 @@ __device__ __forceinline__ void case_pick(int cs, T ll, T l, T r, T rr, T& A, T&
 
 // One velocity component: the along-axis 3-point term plus two cross-axis
 // wall stencils, the pressure difference, and the solver's relaxation.
+// Group of a case by its centre coefficient a: 1 -> 0, 2/3 -> 1, 4/5 -> 2, 6 -> 3.
+__device__ __forceinline__ int case_group(int cs) {
+  return cs == 1 ? 0 : (cs <= 3 ? 1 : (cs <= 5 ? 2 : 3));
+}
+
+// Centre coefficients (-2 + a1) + a2 of a velocity's two cross stencils for
+// the 4 x 4 case groups, with exactly the arithmetic of vel_fast (the table
+// holds the same doubles it would compute).  Filled once per CTA by the FP64
+// kernels, whose FP64 pipe is their bound: three shared-memory reads replace
+// six FP64 additions per voxel.
+__device__ __forceinline__ double group_a(int g) {
+  return g == 0 ? -8.0 : (g == 1 ? -16.0 / 3.0 : (g == 2 ? -5.0 : -2.0));
+}
+
+__device__ __forceinline__ void fill_centre_table(double* tab) {
+  for (int i = threadIdx.x; i < 16; i += blockDim.x)
+    tab[i] = (-2.0 + group_a(i >> 2)) + group_a(i & 3);
+}
+
 template <typename T, int SOLVER>
 __device__ __forceinline__ T vel_fast(T c, T am, T ap, int cs1, T ll1, T l1, T r1, T rr1, int cs2,
-                                      T ll2, T l2, T r2, T rr2, T dp, bool zero) {
+                                      T ll2, T l2, T r2, T rr2, T dp, bool zero,
+                                      const T* ctab = nullptr) {
   const CaseCoef<T> k1 = case_coef<T>(cs1), k2 = case_coef<T>(cs2);
   T A1, B1, A2, B2;
   case_pick<T>(cs1, ll1, l1, r1, rr1, A1, B1);
@@ -143,7 +163,9 @@ __device__ __forceinline__ T vel_fast(T c, T am, T ap, int cs1, T ll1, T l1, T r
   f = fma(k1.cB, B1, f);
   f = fma(k2.cA, A2, f);
   f = fma(k2.cB, B2, f);
-  f = fma(T(-2.0) + k1.a + k2.a, c, f);  // centre coefficient (exact small sums)
+  const T centre = ctab ? ctab[case_group(cs1) * 4 + case_group(cs2)]
+                        : T(-2.0) + k1.a + k2.a;  // centre coefficient (exact small sums)
+  f = fma(centre, c, f);
   const T K = T(kDt / kRe);
   if (SOLVER == 3) {
     // (1 - w) c + w (-dp + f / Re) dt
@@ -157,7 +179,7 @@ __device__ __forceinline__ T vel_fast(T c, T am, T ap, int cs1, T ll1, T l1, T r
 
 template <typename T, int SOLVER>
 __device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un, T& vn, T& wn,
-                                            T& pn) {
+                                            T& pn, const T* ctab = nullptr) {
   int cx, cy, cz;
   decode_cases(code, cx, cy, cz);
   const bool lx = left_solid(cx), ly = left_solid(cy), lz = left_solid(cz);
@@ -168,13 +190,13 @@ __device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un
   if (SOLVER == 1) div0 = ((s.wzp - s.wc) + (s.vyp - s.vc)) + (s.uxp - s.uc);
   // u: along x, cross y (cy) and z (cz)
   un = vel_fast<T, SOLVER>(s.uc, s.uxm, s.uxp, cy, s.uymm, s.uym, s.uyp, s.uypp, cz, s.uzmm,
-                           s.uzm, s.uzp, s.uzpp, dpx, lx);
+                           s.uzm, s.uzp, s.uzpp, dpx, lx, ctab);
   // v: along y, cross x (cx) and z (cz)
   vn = vel_fast<T, SOLVER>(s.vc, s.vym, s.vyp, cx, s.vxmm, s.vxm, s.vxp, s.vxpp, cz, s.vzmm,
-                           s.vzm, s.vzp, s.vzpp, dpy, ly);
+                           s.vzm, s.vzp, s.vzpp, dpy, ly, ctab);
   // w: along z, cross x (cx) and y (cy)
   wn = vel_fast<T, SOLVER>(s.wc, s.wzm, s.wzp, cx, s.wxmm, s.wxm, s.wxp, s.wxpp, cy, s.wymm,
-                           s.wym, s.wyp, s.wypp, dpz, lz);
+                           s.wym, s.wyp, s.wypp, dpz, lz, ctab);
   T div = (SOLVER == 1) ? div0 : ((s.wzp - wn) + (s.vyp - vn)) + (s.uxp - un);
   pn = fma(T(-kC2 * kDt), div, s.pc);
 }
@@ -284,7 +306,8 @@ __device__ __forceinline__ void lin_to_xyz(int lin, const Grid& g, int& x, int& 
 // One voxel of an FP64 sweep (Jacobi phase 0, red 1, black 2) from A into B.
 template <int SOLVER, int PHASE, bool EXACT>
 __device__ __forceinline__ void sweep64_voxel(const Fields<double>& A, const Fields<double>& B,
-                                              const uint8_t* codes, const Grid& g, int lin) {
+                                              const uint8_t* codes, const Grid& g, int lin,
+                                              const double* ctab = nullptr) {
   int x, y, z;
   lin_to_xyz(lin, g, x, y, z);
   if (PHASE && (((x + y + z) & 1) != PHASE - 1)) return;  // (x+y+z) - 6 has the same parity
@@ -295,7 +318,7 @@ __device__ __forceinline__ void sweep64_voxel(const Fields<double>& A, const Fie
   gather<double, PHASE>(s, A, B, c, x, y, z, g, px, pl);
   double un, vn, wn, pn;
   if (EXACT) update_exact<SOLVER>(s, code, un, vn, wn, pn);
-  else update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
+  else update_fast<double, SOLVER>(s, code, un, vn, wn, pn, ctab);
   write_voxel<double, false>(B, c, x, y, z, g, px, pl, un, vn, wn, pn);
 }
 
@@ -352,7 +375,8 @@ __device__ __forceinline__ void write_voxel4(float4* B, long long c, int x, int 
 // implied), so its residual is taken against that stored value.
 template <int SOLVER>
 __device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, float4* R, float4* E,
-                                                  const uint8_t* codes, const Grid& g, int lin) {
+                                                  const uint8_t* codes, const Grid& g, int lin,
+                                                  const double* ctab = nullptr) {
   int x, y, z;
   lin_to_xyz(lin, g, x, y, z);
   int code = codes[((long long)z * g.NY + y) * g.pxc + x];
@@ -360,7 +384,7 @@ __device__ __forceinline__ void dc_residual_voxel(const Fields<double>& X, float
   Stencil<double> s;
   gather<double, 0>(s, X, X, c, x, y, z, g, g.px64, g.pl64);
   double un, vn, wn, pn;
-  update_fast<double, SOLVER>(s, code, un, vn, wn, pn);
+  update_fast<double, SOLVER>(s, code, un, vn, wn, pn, ctab);
   const double pstored = (z == g.NZ - 3) ? __ldg(X.p + c) : s.pc;
   float ru = (float)(un - s.uc), rv = (float)(vn - s.vc), rw = (float)(wn - s.wc),
         rp = (float)(pn - pstored);
