@@ -137,6 +137,26 @@ def test_mixed_precision_converged_k():
     assert abs(rmx.wk33 - ro.wk33) <= 1e-6 * abs(ro.wk33)
 
 
+@pytest.mark.parametrize("solver,bc,eps", [(2, 1, 1e-11), (2, 2, 1e-11), (2, 3, 1e-11),
+                                           (2, 4, 1e-11), (3, 0, 1e-10), (3, 3, 1e-10)])
+def test_mixed_converged_k_every_boundary(solver, bc, eps):
+    """Mixed form, the FP64 default order and the reference order reach the
+    same permeability for every boundary method (solver 3 on a periodic and a
+    walled one: it needs ~50k-80k iterations on this sample)."""
+    g = synth.sphere_pack((20, 20, 20), rmin=2, rmax=4, solid_fraction=0.6, seed=2)
+    kw = dict(boundary_method=bc, solving_algorithm=solver, max_iter=200000, eps=eps,
+              it_eval=100, it_write=100, voxel_size=1e-5)
+    with pm.Problem(g, None, precision="fp64", **kw) as pr:
+        r64 = pr.solve()
+    with pm.Problem(g, None, precision="mixed", **kw) as pr:
+        rmx = pr.solve()
+    ro = OracleProblem(g, bc, solver, 1e-5).calc_flow(200000, 100, 100, eps, "reference")
+    assert r64.converged and rmx.converged and ro.iterations < 200000 - 1
+    for r in (r64, rmx):
+        for a in ("wk13", "wk23", "wk33"):
+            assert abs(getattr(r, a) - getattr(ro, a)) <= 1e-6 * abs(ro.wk33), a
+
+
 def test_mixed_rejects_solver1():
     g = geom_small()
     with pytest.raises(pm.PMError):
