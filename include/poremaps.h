@@ -107,12 +107,20 @@ typedef struct {
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */
+  double eps_fixed_point;       /* 0 (default): stop at conv < eps as the reference does.
+                                   > 0: stop at conv < eps_fixed_point instead, or when
+                                   conv stagnates at its rounding floor: the largest conv
+                                   of a window of 10 evaluations is below eps and no
+                                   smaller than the previous window's.  Both count as
+                                   converged.  Runs the fast orders and the mixed form to
+                                   the fixed point, where their permeability agrees with
+                                   the reference order's to far below eps */
 } pm_params;
 
 typedef struct {
   int iterations;     /* iteration index of the last convergence evaluation */
   int sweeps;         /* sweeps performed (iterations + 1 when stopped by eps) */
-  int converged;      /* 1 if conv < eps stopped the loop */
+  int converged;      /* 1 if the stop rule (conv < eps, or eps_fixed_point's) ended the loop */
   double conv;
   double permeability; /* mean(w)/Re in voxel units (compute_convergence) */
   double k13, k23, k33;        /* dom_interest box (0 if off) */
@@ -167,7 +175,9 @@ pm_status pm_get_neighborhood(pm_problem* pr, int32_t* out);
  * write_output, byte-compatible with the reference writers. */
 pm_status pm_write_outputs(pm_problem* pr);
 
-/* The whole POREMAPS program on one .inp file (log + field files); res may be NULL. */
+/* The whole POREMAPS program on one .inp file (log + field files); res may be NULL.
+ * overrides (may be NULL) supplies the GPU extensions order, precision, arith,
+ * mixed_inner and eps_fixed_point; the .inp supplies everything else. */
 pm_status pm_run_inp(const char* inp_path, const pm_params* overrides, pm_result* res);
 
 /* Full permeability tensor from three axis-rotated solves of one geometry

@@ -50,7 +50,7 @@ class Params(C.Structure):
                 ("dom_interest", C.c_int * 6), ("write_output", C.c_int * 4),
                 ("order", C.c_int), ("precision", C.c_int), ("arith", C.c_int),
                 ("write_log", C.c_int), ("mixed_inner", C.c_int), ("kernel", C.c_int),
-                ("brick", C.c_int * 3)]
+                ("brick", C.c_int * 3), ("eps_fixed_point", C.c_double)]
 
 
 class Result(C.Structure):

@@ -80,6 +80,8 @@ pm_status validate(const pm_params* p) {
   if (p->order < -1 || p->order > 2) return set_error(PM_ERR_INVALID, "bad order %d", p->order);
   if (p->precision < 0 || p->precision > 1)
     return set_error(PM_ERR_INVALID, "bad precision %d", p->precision);
+  if (!(p->eps_fixed_point >= 0) || !isfinite(p->eps_fixed_point))
+    return set_error(PM_ERR_INVALID, "eps_fixed_point must be finite and >= 0");
   {
     const int* b = p->brick;
     const bool none = !b[0] && !b[1] && !b[2], all = b[0] > 0 && b[1] > 0 && b[2] > 0;
@@ -491,6 +493,7 @@ pm_status reset_state(pm_problem* pr) {
   pr->perm_prev = 0.0;
   pr->conv = 0.0;
   pr->conv_valid = false;
+  pr->stop = pm::StopState{};
   pr->first_log = true;
   pr->device_ms = 0.0;
   pr->sweeps_done = 0;
@@ -771,7 +774,8 @@ pm_status pm_solve(pm_problem* pr, pm_result* res) {
   double perm = pr->perm_prev;
   pm_status s = PM_OK;
   float block_ms = 0.f;
-  while (pr->iteration < p.max_iter && conv >= p.eps) {
+  bool done = pr->conv_valid && stop_met(p, conv, pr->stop);
+  while (pr->iteration < p.max_iter && !done) {
     // the next iteration at which the reference evaluates convergence
     long long it = pr->iteration;
     long long nxt = it;
@@ -790,6 +794,8 @@ pm_status pm_solve(pm_problem* pr, pm_result* res) {
     pr->device_ms += block_ms;
     if (check) {
       convergence_from(pr, pr->hout[2], &perm, &conv);
+      stop_record(p, conv, pr->stop);
+      done = stop_met(p, conv, pr->stop);
       res->iterations = (int)last;
       if (last % p.it_write == 0) {
         // the full permeability is only needed for a log row here; the
@@ -814,7 +820,7 @@ pm_status pm_solve(pm_problem* pr, pm_result* res) {
   res->iterations = keep.iterations;
   res->sweeps = (int)pr->sweeps_done;
   res->conv = conv;
-  res->converged = conv < p.eps;
+  res->converged = pr->conv_valid && stop_converged(p, conv, pr->stop);
   res->permeability = perm;
   res->device_ms = pr->device_ms;
   res->wall_ms =

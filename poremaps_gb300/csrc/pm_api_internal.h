@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 
 #include <vector>
 
@@ -9,6 +10,54 @@
 #include "pm_internal.h"
 #include "pm_brick.h"
 #include "pm_zmarch.h"
+
+namespace pm {
+
+// Stop rule of calc_flow: conv < eps, evaluated every it_eval iterations
+// after iteration 1000 (calc_flow.cc:92-168); a NaN conv also stops it.
+// pm_params.eps_fixed_point > 0 replaces eps by that threshold and adds a
+// stagnation stop for thresholds below the rounding floor of conv: the
+// evaluations are grouped in windows of kStallChecks, and the run ends as
+// converged when a window's largest conv is below eps and no smaller than the
+// previous window's.  While conv falls geometrically every window's maximum is
+// below the last one (a single dip of conv, where the change of k passes
+// through zero, does not lower a window's maximum); at the floor, where conv
+// is rounding noise, they stop falling.
+constexpr int kStallChecks = 10;
+
+struct StopState {
+  double win_max = 0.0;          // largest conv of the current window
+  int win_n = 0;                 // evaluations in the current window
+  double prev_max = HUGE_VAL;    // largest conv of the previous window
+  bool stalled = false;
+};
+
+inline double stop_threshold(const pm_params& p) {
+  return p.eps_fixed_point > 0 ? p.eps_fixed_point : p.eps;
+}
+
+// Records one convergence evaluation.
+inline void stop_record(const pm_params& p, double conv, StopState& s) {
+  if (p.eps_fixed_point <= 0 || s.stalled) return;
+  s.win_max = conv > s.win_max ? conv : s.win_max;
+  if (++s.win_n < kStallChecks) return;
+  s.stalled = s.win_max < p.eps && s.win_max >= s.prev_max;
+  s.prev_max = s.win_max;
+  s.win_max = 0.0;
+  s.win_n = 0;
+}
+
+// Whether the loop ends after an evaluation that gave conv.
+inline bool stop_met(const pm_params& p, double conv, const StopState& s) {
+  return !(conv >= stop_threshold(p)) || s.stalled;
+}
+
+// The result's converged flag.
+inline bool stop_converged(const pm_params& p, double conv, const StopState& s) {
+  return isfinite(conv) && (conv < stop_threshold(p) || s.stalled);
+}
+
+}  // namespace pm
 
 // One device-resident domain (the state behind a pm_problem handle).
 struct pm_problem {
@@ -25,8 +74,8 @@ struct pm_problem {
   uint8_t* codes = nullptr;
   int* list = nullptr;
   int nlist = 0;
-  int nred = 0;
-  int pf64[3] = {1, 1, 1};  // per FP64 phase (Jacobi, red, black): persistent sweep  // red-black order: the list holds the red voxels first, then black
+  int nred = 0;             // red-black order: the list holds the red voxels first, then black
+  int pf64[3] = {1, 1, 1};  // per FP64 phase (Jacobi, red, black): persistent sweep
   double* f64_base[2] = {nullptr, nullptr};
   pm::Fields<double> F[2];
   float4* f32_base = nullptr;  // e0, e1, r (interleaved u, v, w, p)
@@ -52,6 +101,7 @@ struct pm_problem {
   double perm_prev = 0.0;
   double conv = 0.0;
   bool conv_valid = false;
+  pm::StopState stop;
   bool first_log = true;
   pm::Counts counts{};
   double phi = 0.0;

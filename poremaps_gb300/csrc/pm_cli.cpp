@@ -2,11 +2,13 @@
 //
 //   poremaps_gpu [file.inp] [--order reference|jacobi|redblack]
 //                [--precision fp64|mixed] [--arith exact|fast]
+//                [--eps-fixed-point X]
 //
 // Reads the same .inp (default input_param.inp, main_stokes_solver.cc:146-147)
 // and .raw geometry, appends the same permeability log rows and writes the
 // same velx_/vely_/velz_/press_/voxel_neighborhood_/domain_decomp_ files.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "../../include/poremaps.h"
@@ -26,6 +28,8 @@ int main(int argc, char** argv) {
       ov.precision = !strcmp(argv[++a], "mixed") ? PM_PREC_MIXED : PM_PREC_FP64;
     } else if (!strcmp(argv[a], "--arith") && a + 1 < argc) {
       ov.arith = !strcmp(argv[++a], "exact") ? PM_ARITH_EXACT : PM_ARITH_FAST;
+    } else if (!strcmp(argv[a], "--eps-fixed-point") && a + 1 < argc) {
+      ov.eps_fixed_point = strtod(argv[++a], nullptr);
     } else if (argv[a][0] != '-') {
       inp = argv[a];
     } else {

@@ -185,6 +185,7 @@ pm_status pm_run_inp(const char* inp_path, const pm_params* overrides, pm_result
     p.precision = overrides->precision;
     p.arith = overrides->arith;
     p.mixed_inner = overrides->mixed_inner;
+    p.eps_fixed_point = overrides->eps_fixed_point;
   }
   p.write_log = 1;
   std::vector<uint8_t> geom((size_t)p.size[0] * p.size[1] * p.size[2]);

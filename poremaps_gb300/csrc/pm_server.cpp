@@ -47,6 +47,7 @@ struct Res {
   size_t bytes;
   double perm = 0.0, conv = 0.0;
   bool conv_valid = false;
+  StopState stop;
   int last_check = 0;
   int it = 0;  // next iteration index
   int item0 = 0, nitems = 0;
@@ -155,7 +156,7 @@ void retire(pm_server* s, Res& r, pm_status st) {
   out.iterations = r.last_check;
   out.sweeps = r.it;
   out.conv = r.conv;
-  out.converged = r.conv_valid && r.conv < p.eps;
+  out.converged = r.conv_valid && stop_converged(p, r.conv, r.stop);
   out.permeability = r.perm;
   if (st == PM_OK && (!isfinite(out.wk33) || !isfinite(r.perm))) st = PM_ERR_NONFINITE;
   complete(s, r.ticket, st, st == PM_OK || st == PM_ERR_NONFINITE ? &out : nullptr, r.submit_ms,
@@ -415,8 +416,9 @@ pm_status after_block(pm_server* s) {
       convergence_from(pr, sum, &r.perm, &r.conv);
       r.conv_valid = true;
       r.last_check = last;
+      stop_record(p, r.conv, r.stop);
     }
-    const bool finished = (r.conv_valid && !(r.conv >= p.eps)) || r.it >= p.max_iter;
+    const bool finished = (r.conv_valid && stop_met(p, r.conv, r.stop)) || r.it >= p.max_iter;
     if (!finished && r.it + s->block <= p.max_iter) {
       keep.push_back(r);
       continue;

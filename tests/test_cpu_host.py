@@ -46,6 +46,7 @@ def test_version_and_defaults(lib):
     p = pm.default_params()
     assert p.eps == 1e-6 and p.porosity == -1.0 and p.it_eval == 100
     assert p.order == pm.ORDER_DEFAULT and p.precision == pm.PREC_FP64
+    assert p.eps_fixed_point == 0.0
 
 
 TEMPLATE = """dom_decomposition 0 0 0
@@ -111,7 +112,8 @@ def test_read_geometry(lib, tmp_path):
 def test_problem_create_validates_before_touching_the_device(lib):
     g = np.zeros((4, 4, 4), np.uint8)
     for kw in (dict(boundary_method=5), dict(solving_algorithm=4), dict(it_eval=0),
-               dict(solving_algorithm=1, precision="mixed")):
+               dict(solving_algorithm=1, precision="mixed"), dict(eps_fixed_point=-1e-9),
+               dict(eps_fixed_point=float("nan"))):
         with pytest.raises(pm.PMError) as e:
             pm.Problem(g, None, **kw)
         assert e.value.status == 1

@@ -71,6 +71,22 @@ def test_cli_mixed_precision_converges_to_reference_k(tmp_path):
         assert (tmp_path / (pre + "geom.raw")).stat().st_size == 8 * 20 * 20 * 20
 
 
+def test_cli_eps_fixed_point(tmp_path):
+    """poremaps_gpu --precision mixed --eps-fixed-point 1e-30: the run goes on
+    past the reference's eps stop to the rounding floor of conv and ends
+    there; its permeability is the reference program's to its 7 digits."""
+    log = run_cli("spheres_converged", tmp_path,
+                  ["--precision", "mixed", "--eps-fixed-point", "1e-30"])
+    rows = [r for r in log.strip().splitlines() if not r.startswith("#")]
+    ref_rows = [r for r in str(GOLDEN["spheres_converged/log"]).strip().splitlines()
+                if not r.startswith("#")]
+    last = [c.strip() for c in rows[-1].split(",")]
+    ref = [c.strip() for c in ref_rows[-1].split(",")]
+    assert len(rows) > len(ref_rows) and int(last[0]) < 200000 - 1
+    assert float(last[1]) < 1e-10
+    assert abs(float(last[-1]) - float(ref[-1])) <= 2e-6 * abs(float(ref[-1]))
+
+
 def test_c1_cylinder_full_calc_flow_reference_order():
     """48x48x64 cylinder r=20, GS, eps 1e-6: the reference stops at iteration
     64,200 with wk33 = 1.070459e-08 m^2 (Hagen-Poiseuille 1.0908e-08)."""

@@ -157,6 +157,28 @@ def test_mixed_converged_k_every_boundary(solver, bc, eps):
             assert abs(getattr(r, a) - getattr(ro, a)) <= 1e-6 * abs(ro.wk33), a
 
 
+@pytest.mark.parametrize("kw", [dict(order="redblack"), dict(order="jacobi"),
+                                dict(precision="mixed")])
+def test_eps_fixed_point_reaches_the_reference_fixed_point(kw):
+    """eps_fixed_point below the rounding floor: the run ends by stagnation,
+    converged, on the reference order's fixed point to ~1e-10 (at eps = 1e-6
+    the orders stop ~1e-5 apart)."""
+    g = synth.sphere_pack((20, 20, 20), rmin=2, rmax=4, solid_fraction=0.6, seed=2)
+    base = dict(boundary_method=0, solving_algorithm=2, max_iter=200000, eps=1e-6,
+                it_eval=100, it_write=100, voxel_size=1e-5)
+    with pm.Problem(g, None, eps_fixed_point=1e-30, **base, **kw) as pr:
+        r = pr.solve()
+    ro = OracleProblem(g, 0, 2, 1e-5).calc_flow(200000, 100, 100, 1e-15, "reference")
+    assert r.converged and r.iterations < 60000 and r.conv < 1e-6
+    assert abs(r.wk33 - ro.wk33) <= 1e-10 * abs(ro.wk33)
+    for a in ("wk13", "wk23"):
+        assert abs(getattr(r, a) - getattr(ro, a)) <= 1e-10 * abs(ro.wk33), a
+    # a reachable threshold stops at it
+    with pm.Problem(g, None, eps_fixed_point=1e-12, **base, **kw) as pr:
+        r12 = pr.solve()
+    assert r12.converged and r12.conv < 1e-12 and r12.iterations <= r.iterations
+
+
 def test_mixed_rejects_solver1():
     g = geom_small()
     with pytest.raises(pm.PMError):

@@ -202,3 +202,27 @@ def test_mixed_solvers_in_one_batch():
         assert c.status == 0 and c.result.iterations == r.iterations
         for a in ("wk13", "wk23", "wk33"):
             assert getattr(c.result, a) == getattr(r, a), (i, a)
+
+
+def test_server_eps_fixed_point_matches_single_problem():
+    """The fixed-point stop rule in the server.  A threshold well above the
+    rounding floor of conv stops at the same iteration as pm_solve.  Below the
+    floor the run ends by stagnation, and where exactly depends on conv's last
+    bits, which the server sums in another order (per-item partials) than
+    pm_solve: both stop within a few windows of evaluations of each other, on
+    the same fixed point."""
+    geoms = samples(3, seed=4)
+    kw = dict(eps_fixed_point=1e-11, max_iter=200000)
+    res = run_server(geoms, kw=kw)
+    for i, g in enumerate(geoms):
+        c, r = res[i], single(g, kw=kw)
+        assert c.status == 0 and c.result.converged and r.converged
+        assert c.result.iterations == r.iterations and c.result.sweeps == r.sweeps
+        assert c.result.wk33 == r.wk33 and c.result.conv < 1e-11
+    kw = dict(eps_fixed_point=1e-30, max_iter=200000)
+    res = run_server(geoms, kw=kw)
+    for i, g in enumerate(geoms):
+        c, r = res[i], single(g, kw=kw)
+        assert c.status == 0 and c.result.converged and r.converged
+        assert c.result.iterations < 100000 and abs(c.result.iterations - r.iterations) <= 5000
+        assert abs(c.result.wk33 - r.wk33) <= 1e-12 * abs(r.wk33)
