@@ -110,7 +110,7 @@ typedef struct {
   double eps_fixed_point;       /* 0 (default): stop at conv < eps as the reference does.
                                    > 0: stop at conv < eps_fixed_point instead, or when
                                    conv stagnates at its rounding floor: the largest conv
-                                   of a window of 10 evaluations is below eps and no
+                                   of a window of 10 evaluations is below 1e-13 and no
                                    smaller than the previous window's.  Both count as
                                    converged.  Runs the fast orders and the mixed form to
                                    the fixed point, where their permeability agrees with
