@@ -58,10 +58,7 @@ pm_status cuda_error(cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return cuda_error(_e, #expr); \
   } while (0)
 
-
 namespace {
-
-long long align_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
 pm_status validate(const pm_params* p) {
   if (!p) return set_error(PM_ERR_INVALID, "params is NULL");
