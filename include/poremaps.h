@@ -134,7 +134,14 @@ typedef struct {
 
 typedef struct pm_problem pm_problem;
 
+/* The calling thread's last error message (thread-local; valid until that
+ * thread's next failing call). */
 const char* pm_last_error(void);
+/* The same message copied into a caller-owned buffer, NUL-terminated and
+ * truncated to size - 1 bytes (nothing is written when size is 0); returns
+ * the full message length.  For bindings that cannot hold a pointer into the
+ * library (cgo, JNI). */
+size_t pm_last_error_copy(char* buf, size_t size);
 const char* pm_version(void);
 pm_status pm_params_default(pm_params* p);
 

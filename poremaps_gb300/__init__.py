@@ -76,7 +76,7 @@ class Completion(C.Structure):
 
 
 # Every symbol declared in include/poremaps.h (checked by the CPU tests).
-EXPORTS = ["pm_last_error", "pm_version", "pm_params_default", "pm_read_params",
+EXPORTS = ["pm_last_error", "pm_last_error_copy", "pm_version", "pm_params_default", "pm_read_params",
            "pm_read_geometry", "pm_problem_create", "pm_problem_destroy", "pm_solve",
            "pm_iterate", "pm_compute_convergence", "pm_compute_permeability", "pm_get_porosity",
            "pm_get_iteration", "pm_get_fields", "pm_set_fields", "pm_resume_outputs",
@@ -103,6 +103,7 @@ def load_library(path: str = LIB_PATH):
     vp = C.c_void_p
     sig = {
         "pm_last_error": (C.c_char_p, []),
+        "pm_last_error_copy": (C.c_size_t, [C.c_char_p, C.c_size_t]),
         "pm_version": (C.c_char_p, []),
         "pm_params_default": (C.c_int, [P(Params)]),
         "pm_read_params": (C.c_int, [C.c_char_p, P(Params)]),

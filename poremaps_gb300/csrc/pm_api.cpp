@@ -572,6 +572,15 @@ size_t problem_device_bytes(const pm_params* p) {
 extern "C" {
 
 const char* pm_last_error(void) { return g_err.c_str(); }
+size_t pm_last_error_copy(char* buf, size_t size) {
+  const size_t n = g_err.size();
+  if (buf && size > 0) {
+    const size_t k = n < size - 1 ? n : size - 1;
+    memcpy(buf, g_err.data(), k);
+    buf[k] = '\0';
+  }
+  return n;
+}
 const char* pm_version(void) { return "poremaps_gb300 0.1 (sm_103a)"; }
 
 pm_status pm_params_default(pm_params* p) {

@@ -29,7 +29,7 @@ def lib():
 
 def header_symbols():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:pm_status|const char\*|double|uint64_t)\s+(pm_\w+)\(",
+    return sorted(set(re.findall(r"^\s*(?:pm_status|const char\*|double|uint64_t|size_t)\s+(pm_\w+)\(",
                                  src, re.M)))
 
 
@@ -107,6 +107,21 @@ def test_read_geometry(lib, tmp_path):
     assert np.array_equal(out.reshape(g.shape), g)
     size2 = (C.c_int * 3)(3, 4, 6)  # file too short
     assert lib.pm_read_geometry(str(path).encode(), size2, out.ctypes.data) == 2
+
+
+def test_last_error_copy(lib):
+    """The message of the last failing call, copied into a caller buffer:
+    truncated and NUL-terminated, full length returned."""
+    with pytest.raises(pm.PMError):
+        pm.Problem(np.zeros((4, 4, 4), np.uint8), None, boundary_method=5)
+    msg = lib.pm_last_error()
+    assert b"boundary_method" in msg
+    buf = C.create_string_buffer(b"x" * 16, 16)
+    n = lib.pm_last_error_copy(buf, 16)
+    assert n == len(msg) and buf.value == msg[:15] and buf.raw[15:16] == b"\0"
+    big = C.create_string_buffer(n + 8)
+    assert lib.pm_last_error_copy(big, n + 8) == n and big.value == msg
+    assert lib.pm_last_error_copy(None, 0) == n
 
 
 def test_problem_create_validates_before_touching_the_device(lib):
