@@ -38,6 +38,8 @@ typedef struct {
   double *u, *v, *w, *p;
   double *u2, *v2, *w2, *p2;
   double* p3; /* swept (pre-reapply) pressure of the last interior plane */
+  unsigned short* ck; /* neighbourhood cases of nh decoded once: cx | cy << 4 | cz << 8 */
+  double* stage;      /* z-exchange send planes: 4 fields x (low 2 + high 2) planes */
 } slab;
 
 struct or_problem {
@@ -149,6 +151,16 @@ static void eval_geometry(slab* S) {
           else if (l == 0 && r == 0) cs = 6;
           S->nh[c] += cs * shift[d];
         }
+  /* split_number (solver.cc:94-109) of every fluid code, done here once
+   * instead of per voxel and sweep (the same integer digits) */
+  for (long c = 0; c < n; ++c) {
+    int code = S->nh[c];
+    if (code <= 0) { S->ck[c] = 0; continue; }
+    int cz = code % 10; code /= 10;
+    int cy = code % 10; code /= 10;
+    int cx = code % 10;
+    S->ck[c] = (unsigned short)(cx | (cy << 4) | (cz << 8));
+  }
 }
 
 /* ---------------------------------------------------------------------- */
@@ -202,10 +214,8 @@ static inline void voxel(const slab* S, long c, unsigned solver, const double* s
   double dp_dz = g[c - sz] == 0 ? -sp[c - sz] + sp[c] : 0.;
   double dp_dy = g[c - sy] == 0 ? -pym + sp[c] : 0.;
   double dp_dx = g[c - sx] == 0 ? -pxm + sp[c] : 0.;
-  int code = S->nh[c];
-  int cz = code % 10; code /= 10;
-  int cy = code % 10; code /= 10;
-  int cx = code % 10;
+  const unsigned ck = S->ck[c];
+  const int cx = ck & 15, cy = (ck >> 4) & 15, cz = ck >> 8;
   double uxx = (su[c - sx] - 2 * su[c] + su[c + sx]);
   double vyy = (sv[c - sy] - 2 * sv[c] + sv[c + sy]);
   double wzz = (sw[c - sz] - 2 * sw[c] + sw[c + sz]);
@@ -239,7 +249,8 @@ static inline void voxel(const slab* S, long c, unsigned solver, const double* s
   dpr[c] = sp[c] - C2 * v_sum * DT;
 }
 
-/* central_diff5 (solver.cc:112-224): in-place lexicographic sweep. */
+/* central_diff5 (solver.cc:112-224): in-place lexicographic sweep of one
+ * slab (one rank of the reference run). */
 static void sweep_reference(or_problem* pr, slab* S) {
   for (int i = LIM; i < S->NZ - LIM; i++)
     for (int j = LIM; j < S->NY - LIM; j++)
@@ -264,18 +275,21 @@ static void save_p3(slab* S) {
   memcpy(S->p3, S->p + (long)(S->NZ - 3) * plane, sizeof(double) * plane);
 }
 
-static void copy_state(slab* S) {
-  size_t n = sizeof(double) * S->NX * S->NY * S->NZ;
-  memcpy(S->u2, S->u, n); memcpy(S->v2, S->v, n);
-  memcpy(S->w2, S->w, n); memcpy(S->p2, S->p, n);
+/* state2 := state on padded planes [z0, z1) */
+static void copy_planes(slab* S, int z0, int z1) {
+  if (z1 <= z0) return;
+  long plane = (long)S->NX * S->NY, o = (long)z0 * plane;
+  size_t n = sizeof(double) * plane * (z1 - z0);
+  memcpy(S->u2 + o, S->u + o, n); memcpy(S->v2 + o, S->v + o, n);
+  memcpy(S->w2 + o, S->w + o, n); memcpy(S->p2 + o, S->p + o, n);
 }
 
-/* Ping-pong Jacobi ordering of the same update: every neighbour is read from
- * the previous iterate; solvers 2/3 use the voxel's own new velocity in the
- * divergence exactly as solver.cc:216-218 does. */
-static void sweep_jacobi(or_problem* pr, slab* S) {
-  copy_state(S);
-  for (int i = LIM; i < S->NZ - LIM; i++)
+/* Ping-pong Jacobi ordering of the same update on interior planes [i0, i1):
+ * every neighbour is read from the previous iterate; solvers 2/3 use the
+ * voxel's own new velocity in the divergence exactly as solver.cc:216-218
+ * does. */
+static void jacobi_planes(or_problem* pr, slab* S, int i0, int i1) {
+  for (int i = i0; i < i1; i++)
     for (int j = LIM; j < S->NY - LIM; j++)
       for (int k = LIM; k < S->NX - LIM; k++) {
         long c = IDX(S, i, j, k);
@@ -283,32 +297,31 @@ static void sweep_jacobi(or_problem* pr, slab* S) {
           voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u2, S->v2, S->w2, S->p2,
                 i == S->NZ - 3 ? S->p3 : NULL);
       }
-  swap_state(S);
-  save_p3(S);
 }
 
 /* Red-black ordering: colour = parity of the global interior coordinates.
- * Red voxels update from the previous iterate; black voxels then update from
- * the state holding the new red values and the old black values (so the
- * same-colour +-2 reads of the wall stencils see old values and the result
- * does not depend on the order inside a colour). */
-static void sweep_redblack(or_problem* pr, slab* S) {
-  copy_state(S); /* state2 := state */
-  for (int colour = 0; colour < 2; ++colour)
-    for (int i = LIM; i < S->NZ - LIM; i++)
-      for (int j = LIM; j < S->NY - LIM; j++)
-        for (int k = LIM; k < S->NX - LIM; k++) {
-          if ((((k - LIM) + (j - LIM) + (S->z0 + i - LIM)) & 1) != colour) continue;
-          long c = IDX(S, i, j, k);
-          if (S->g[c] != 0) continue;
-          if (colour == 0) /* red: old state -> state2; black neighbours' swept p */
-            voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u2, S->v2, S->w2, S->p2,
-                  i == S->NZ - 3 ? S->p3 : NULL);
-          else /* black: state2 (new red, old black) -> state */
-            voxel(S, c, pr->solver, S->u2, S->v2, S->w2, S->p2, S->u, S->v, S->w, S->p, NULL);
-        }
-  /* merge the new red values into state */
-  for (int i = LIM; i < S->NZ - LIM; i++)
+ * Red voxels update from the previous iterate (state -> state2); black
+ * voxels then update from state2, which holds the new red values and the old
+ * black values (so the same-colour +-2 reads of the wall stencils see old
+ * values and the result does not depend on the order inside a colour), into
+ * state; finally the new red values are merged into state. */
+static void colour_planes(or_problem* pr, slab* S, int colour, int i0, int i1) {
+  for (int i = i0; i < i1; i++)
+    for (int j = LIM; j < S->NY - LIM; j++)
+      for (int k = LIM; k < S->NX - LIM; k++) {
+        if ((((k - LIM) + (j - LIM) + (S->z0 + i - LIM)) & 1) != colour) continue;
+        long c = IDX(S, i, j, k);
+        if (S->g[c] != 0) continue;
+        if (colour == 0) /* red: old state -> state2; black neighbours' swept p */
+          voxel(S, c, pr->solver, S->u, S->v, S->w, S->p, S->u2, S->v2, S->w2, S->p2,
+                i == S->NZ - 3 ? S->p3 : NULL);
+        else /* black: state2 (new red, old black) -> state */
+          voxel(S, c, pr->solver, S->u2, S->v2, S->w2, S->p2, S->u, S->v, S->w, S->p, NULL);
+      }
+}
+
+static void merge_red_planes(slab* S, int i0, int i1) {
+  for (int i = i0; i < i1; i++)
     for (int j = LIM; j < S->NY - LIM; j++)
       for (int k = LIM; k < S->NX - LIM; k++) {
         if (((k - LIM) + (j - LIM) + (S->z0 + i - LIM)) & 1) continue;
@@ -316,37 +329,179 @@ static void sweep_redblack(or_problem* pr, slab* S) {
         if (S->g[c] != 0) continue;
         S->u[c] = S->u2[c]; S->v[c] = S->v2[c]; S->w[c] = S->w2[c]; S->p[c] = S->p2[c];
       }
-  save_p3(S);
 }
 
-typedef struct { or_problem* pr; int order; int first, step; } sweep_job;
+static double* field_of(slab* S, int f) {
+  return f == 0 ? S->p : f == 1 ? S->u : f == 2 ? S->v : S->w;
+}
 
-static void* sweep_worker(void* arg) {
-  sweep_job* jb = (sweep_job*)arg;
-  for (int c = jb->first; c < jb->pr->ns; c += jb->step) {
-    slab* S = &jb->pr->s[c];
-    if (jb->order == OR_ORDER_REFERENCE) sweep_reference(jb->pr, S);
-    else if (jb->order == OR_ORDER_JACOBI) sweep_jacobi(jb->pr, S);
-    else sweep_redblack(jb->pr, S);
+/* communicate_halos (parallelization.cc:193-318), x and y part, on padded
+ * planes [z0, z1) of one field: on one rank in x/y the neighbour is the
+ * slab itself (periodic) or none.  x then y per plane, as the reference's
+ * X-then-Y order leaves them (the y copies carry the x halos). */
+static void exchange_xy_planes(or_problem* pr, slab* S, double* a, int z0, int z1) {
+  int nx = S->NX, ny = S->NY;
+  for (int i = z0; i < z1; i++) {
+    if (pr->periods[0])
+      for (int j = 0; j < ny; j++) {
+        double s2 = a[IDX(S, i, j, 2)], s3 = a[IDX(S, i, j, 3)];
+        double r0 = a[IDX(S, i, j, nx - 4)], r1 = a[IDX(S, i, j, nx - 3)];
+        a[IDX(S, i, j, nx - 2)] = s2; a[IDX(S, i, j, nx - 1)] = s3;
+        a[IDX(S, i, j, 0)] = r0; a[IDX(S, i, j, 1)] = r1;
+      }
+    if (pr->periods[1])
+      for (int k = 0; k < nx; k++) {
+        double s2 = a[IDX(S, i, 2, k)], s3 = a[IDX(S, i, 3, k)];
+        double r0 = a[IDX(S, i, ny - 4, k)], r1 = a[IDX(S, i, ny - 3, k)];
+        a[IDX(S, i, ny - 2, k)] = s2; a[IDX(S, i, ny - 1, k)] = s3;
+        a[IDX(S, i, 0, k)] = r0; a[IDX(S, i, 1, k)] = r1;
+      }
+  }
+}
+
+/* z part: every slab first packs its send planes (2, 3 down; NZ-4, NZ-3 up)
+ * for all four fields (MPI_Sendrecv semantics), then receives the adjacent
+ * slabs' planes into its halos (wrapping when z is periodic). */
+static void exchange_z_pack(slab* S) {
+  long plane = (long)S->NX * S->NY;
+  for (int f = 0; f < 4; ++f) {
+    double* a = field_of(S, f);
+    memcpy(S->stage + (long)(4 * f) * plane, a + 2 * plane, sizeof(double) * 2 * plane);
+    memcpy(S->stage + (long)(4 * f + 2) * plane, a + (long)(S->NZ - 4) * plane,
+           sizeof(double) * 2 * plane);
+  }
+}
+
+static void exchange_z_unpack(or_problem* pr, int c) {
+  slab* S = &pr->s[c];
+  long plane = (long)S->NX * S->NY;
+  int ns = pr->ns, up = c + 1, dn = c - 1;
+  if (up == ns) up = pr->periods[2] ? 0 : -1;
+  if (dn < 0) dn = pr->periods[2] ? ns - 1 : -1;
+  for (int f = 0; f < 4; ++f) {
+    double* a = field_of(S, f);
+    if (up >= 0)
+      memcpy(a + (long)(S->NZ - 2) * plane, pr->s[up].stage + (long)(4 * f) * plane,
+             sizeof(double) * 2 * plane);
+    if (dn >= 0)
+      memcpy(a, pr->s[dn].stage + (long)(4 * f + 2) * plane, sizeof(double) * 2 * plane);
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Iteration engine.  One calc_flow iteration (calc_flow.cc:101-118) is
+ * [reapply before the first] -> sweep -> halo exchange of p, u, v, w ->
+ * reapply.  nthreads workers run a block of iterations with a barrier after
+ * every phase:
+ *   - reference order: each worker sweeps whole slabs (a slab is a rank of
+ *     the reference run, its in-place sweep is sequential);
+ *   - Jacobi / red-black: each pass reads only the other buffer, so the
+ *     workers split every slab's z planes;
+ *   - exchange: x/y copies split by planes, z copies by slab.
+ * Every phase completes before the next starts, so the values are bitwise
+ * those of one worker. */
+typedef struct {
+  or_problem* pr;
+  int order, n, tid, nt;
+  pthread_barrier_t* bar;
+} pool_job;
+
+static void pool_wait(pool_job* jb) {
+  if (jb->nt > 1) pthread_barrier_wait(jb->bar);
+}
+
+static inline void part(int lo, int hi, int t, int nt, int* a, int* b) {
+  long n = hi - lo;
+  *a = lo + (int)(n * t / nt);
+  *b = lo + (int)(n * (t + 1) / nt);
+}
+
+static void* pool_worker(void* arg) {
+  pool_job* jb = (pool_job*)arg;
+  or_problem* pr = jb->pr;
+  const int t = jb->tid, nt = jb->nt, ns = pr->ns;
+  int a, b;
+  for (int it = 0; it < jb->n; ++it) {
+    if (pr->iteration == 0) {
+      if (t == 0) reapply(pr);
+      pool_wait(jb);
+    }
+    if (jb->order == OR_ORDER_REFERENCE) {
+      for (int c = t; c < ns; c += nt) sweep_reference(pr, &pr->s[c]);
+      pool_wait(jb);
+    } else {
+      for (int c = 0; c < ns; ++c) {
+        part(0, pr->s[c].NZ, t, nt, &a, &b);
+        copy_planes(&pr->s[c], a, b);
+      }
+      pool_wait(jb);
+      if (jb->order == OR_ORDER_JACOBI) {
+        for (int c = 0; c < ns; ++c) {
+          slab* S = &pr->s[c];
+          part(LIM, S->NZ - LIM, t, nt, &a, &b);
+          jacobi_planes(pr, S, a, b);
+        }
+        pool_wait(jb);
+        if (t == 0)
+          for (int c = 0; c < ns; ++c) swap_state(&pr->s[c]);
+      } else {
+        for (int colour = 0; colour < 2; ++colour) {
+          for (int c = 0; c < ns; ++c) {
+            slab* S = &pr->s[c];
+            part(LIM, S->NZ - LIM, t, nt, &a, &b);
+            colour_planes(pr, S, colour, a, b);
+          }
+          pool_wait(jb);
+        }
+        for (int c = 0; c < ns; ++c) {
+          slab* S = &pr->s[c];
+          part(LIM, S->NZ - LIM, t, nt, &a, &b);
+          merge_red_planes(S, a, b);
+        }
+      }
+      pool_wait(jb);
+      if (t == 0)
+        for (int c = 0; c < ns; ++c) save_p3(&pr->s[c]);
+      pool_wait(jb);
+    }
+    for (int c = 0; c < ns; ++c) {
+      slab* S = &pr->s[c];
+      part(0, S->NZ, t, nt, &a, &b);
+      for (int f = 0; f < 4; ++f) exchange_xy_planes(pr, S, field_of(S, f), a, b);
+    }
+    pool_wait(jb);
+    for (int c = t; c < ns; c += nt) exchange_z_pack(&pr->s[c]);
+    pool_wait(jb);
+    for (int c = t; c < ns; c += nt) exchange_z_unpack(pr, c);
+    pool_wait(jb);
+    if (t == 0) {
+      reapply(pr);
+      pr->iteration++;
+    }
+    pool_wait(jb);
   }
   return NULL;
 }
 
-static void sweep_all(or_problem* pr, int order) {
-  int nt = pr->nthreads < pr->ns ? pr->nthreads : pr->ns;
+/* n iterations on the worker pool (the calling thread is worker 0). */
+static void run_iterations(or_problem* pr, int order, int n) {
+  if (n <= 0) return;
+  int nt = pr->nthreads;
+  if (nt > 256) nt = 256;
   if (nt <= 1) {
-    sweep_job jb = {pr, order, 0, 1};
-    sweep_worker(&jb);
+    pool_job jb = {pr, order, n, 0, 1, NULL};
+    pool_worker(&jb);
     return;
   }
+  pthread_barrier_t bar;
+  pthread_barrier_init(&bar, NULL, (unsigned)nt);
   pthread_t th[256];
-  sweep_job jobs[256];
-  if (nt > 256) nt = 256;
-  for (int t = 0; t < nt; ++t) {
-    jobs[t] = (sweep_job){pr, order, t, nt};
-    pthread_create(&th[t], NULL, sweep_worker, &jobs[t]);
-  }
-  for (int t = 0; t < nt; ++t) pthread_join(th[t], NULL);
+  pool_job jobs[256];
+  for (int t = 0; t < nt; ++t) jobs[t] = (pool_job){pr, order, n, t, nt, &bar};
+  for (int t = 1; t < nt; ++t) pthread_create(&th[t], NULL, pool_worker, &jobs[t]);
+  pool_worker(&jobs[0]);
+  for (int t = 1; t < nt; ++t) pthread_join(th[t], NULL);
+  pthread_barrier_destroy(&bar);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -381,6 +536,8 @@ or_problem* or_create(const int size[3], int bc_method, unsigned solver, int nsl
     S->u2 = (double*)calloc(n, 8); S->v2 = (double*)calloc(n, 8);
     S->w2 = (double*)calloc(n, 8); S->p2 = (double*)calloc(n, 8);
     S->p3 = (double*)calloc((long)S->NX * S->NY, 8);
+    S->ck = (unsigned short*)calloc(n, sizeof(unsigned short));
+    S->stage = (double*)calloc((long)16 * S->NX * S->NY, 8);
     for (int i = 0; i < S->lnz; ++i)
       for (int j = 0; j < size[1]; ++j)
         for (int k = 0; k < size[0]; ++k)
@@ -419,7 +576,7 @@ void or_destroy(or_problem* pr) {
     free(S->g); free(S->nh);
     free(S->u); free(S->v); free(S->w); free(S->p);
     free(S->u2); free(S->v2); free(S->w2); free(S->p2);
-    free(S->p3);
+    free(S->p3); free(S->ck); free(S->stage);
   }
   free(pr->s);
   free(pr);
@@ -541,21 +698,26 @@ static double now_s(void) {
   return ts.tv_sec + 1e-9 * ts.tv_nsec;
 }
 
-static void one_iteration(or_problem* pr, int order) {
-  if (pr->iteration == 0) reapply(pr);
-  sweep_all(pr, order);
-  for (int f = 0; f < 4; ++f) exchange_field(pr, f);
-  reapply(pr);
-}
+void or_iterate(or_problem* pr, int order, int n) { run_iterations(pr, order, n); }
 
-void or_iterate(or_problem* pr, int order, int n) {
-  for (int t = 0; t < n; ++t) {
-    one_iteration(pr, order);
-    pr->iteration++;
+/* The next iteration index >= it at which calc_flow evaluates convergence
+ * (it % it_eval == 0 && it > 1000, calc_flow.cc:120). */
+static int next_eval(int it, int it_eval) {
+  if (it_eval <= 0) return 2147483647;
+  int e = it <= 1001 ? 1001 : it;
+  int r = e % it_eval;
+  if (r) {
+    long q = (long)e + (it_eval - r);
+    e = q > 2147483647 ? 2147483647 : (int)q;
   }
+  return e;
 }
 
-/* calc_flow: calc_flow.cc:53-169, including the log rows of output.cc:193-230 */
+/* calc_flow: calc_flow.cc:53-169, including the log rows of output.cc:193-230.
+ * Iterations between two convergence evaluations run as one block on the
+ * worker pool; the stop rule is only consulted at the evaluations, as in the
+ * reference loop, so the trajectory and the stop iteration are the same.
+ * The log's TPS column is the block's mean rate (it is wall-clock time). */
 void or_calc_flow(or_problem* pr, int order, int max_iter, int it_eval, int it_write, double eps,
                   const char* log_path, or_result* res) {
   double conv = 1.0 + eps, perm = 0.0;
@@ -563,30 +725,30 @@ void or_calc_flow(or_problem* pr, int order, int max_iter, int it_eval, int it_w
   memset(res, 0, sizeof(*res));
   while (pr->iteration < max_iter && conv >= eps) {
     int it = pr->iteration;
+    int e = next_eval(it, it_eval);
+    int last = e < max_iter - 1 ? e : max_iter - 1;
     double t0 = now_s();
-    one_iteration(pr, order);
-    if (it % it_eval == 0 && it > 1000) {
-      conv = or_convergence(pr, &perm);
-      if (it % it_write == 0) {
-        or_permeability(pr, res);
-        if (log_path) {
-          double tps = 1.0 / (now_s() - t0);
-          FILE* f = fopen(log_path, "a");
-          if (f) {
-            if (first)
-              fprintf(f, "# iteration, conv, TPS [1/s], wmax_velz [m/s], wmean_velz [m/s], k13 "
-                         "[m^2], k23 [m^2], k33 [m^2], wk13 [m^2], wk23 [m^2], wk33 [m^2]\n");
-            fprintf(f, "%i, %e, %e, %e, %e, %e, %e, %e, %e, %e, %e\n", it, conv, tps,
-                    res->wmax_velz, res->wmean_velz, res->k13, res->k23, res->k33, res->wk13,
-                    res->wk23, res->wk33);
-            fclose(f);
-          }
+    run_iterations(pr, order, last - it + 1);
+    if (last != e) break; /* max_iter reached before the next evaluation */
+    conv = or_convergence(pr, &perm);
+    if (e % it_write == 0) {
+      or_permeability(pr, res);
+      if (log_path) {
+        double tps = (last - it + 1) / (now_s() - t0);
+        FILE* f = fopen(log_path, "a");
+        if (f) {
+          if (first)
+            fprintf(f, "# iteration, conv, TPS [1/s], wmax_velz [m/s], wmean_velz [m/s], k13 "
+                       "[m^2], k23 [m^2], k33 [m^2], wk13 [m^2], wk23 [m^2], wk33 [m^2]\n");
+          fprintf(f, "%i, %e, %e, %e, %e, %e, %e, %e, %e, %e, %e\n", e, conv, tps,
+                  res->wmax_velz, res->wmean_velz, res->k13, res->k23, res->k33, res->wk13,
+                  res->wk23, res->wk33);
+          fclose(f);
         }
-        first = 0;
       }
-      res->iterations = it;
+      first = 0;
     }
-    pr->iteration++;
+    res->iterations = e;
   }
   /* the result reports the permeability of the final state (the log rows keep
    * the values of their own iterations) */
