@@ -46,6 +46,12 @@ def parse():
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the batched-stream (c4) and request-stream (c5) legs that the "
+                         "default single-GPU run adds to its line")
+    ap.add_argument("--c4-samples", type=int, default=256)
+    ap.add_argument("--c5-requests", type=int, default=48)
+    ap.add_argument("--c5-max-axis", type=int, default=192)
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2: 128^3 tensor workload (default); c3: one 512^3 sample "
                          "(HBM-streaming roofline); c4: batched uneven samples; c5: serving "
@@ -63,6 +69,8 @@ def parse():
                     help="c3 --converge: pm_params.eps_fixed_point (0: stop at eps 1e-6 as "
                          "calc_flow; > 0: run every form on to that threshold or to the "
                          "rounding floor of conv)")
+    ap.add_argument("--write-traffic", default=None, metavar="NCU_CSV",
+                    help="write the traffic record of --kernel/--brick from an ncu CSV and exit")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                     help="run two it_eval blocks of one resident problem and exit (a small, "
                          "self-contained case for ncu captures)")
@@ -282,17 +290,18 @@ def run_gpu(args):
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = nvox * ALGO_BYTES_MIXED_INNER / (kernel_ms * 1e-3) / 1e9
-    traffic = None
-    # DRAM bytes of one launch of the chosen kernel on this workload, from an
-    # ncu capture of `bench.py --profile-case mixed` (profiles/*_traffic.json)
-    tpath = os.path.join(ROOT, "profiles", f"{kshort}_sphere{args.size}_traffic.json")
-    if os.path.exists(tpath):
-        t = json.load(open(tpath))
-        traffic = t["dram_bytes_per_launch"] * nvox / t["nvox"]
+    brick = list(probs_mx[2].brick())
+    traffic, traffic_note = kernel_traffic(kid, brick, args.size, nvox)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
+                "frac_dram": (traffic / (kernel_ms * 1e-3) / 1e9 / peak) if traffic else None,
+                "traffic_source": traffic_note,
+                "model": "achieved/frac: dense model (every voxel of the unpadded domain, "
+                         f"{ALGO_BYTES_MIXED_INNER} B); frac_dram: the chosen kernel's measured "
+                         "DRAM bytes per launch over the same CUDA-event launch time. The "
+                         "fluid-list sweep skips solid regions, so the dense model can exceed 1",
                 "kernel": kname, "kernel_choice": "autotuned at problem creation",
-                "kernel_id": kid, "brick": list(probs_mx[2].brick()),
+                "kernel_id": kid, "brick": brick,
                 "kernels_per_rotation": [[KERNELS[p.kernel()][0], list(p.brick())]
                                          for p in probs_mx],
                 "algorithmic_bytes_per_lup": ALGO_BYTES_MIXED_INNER,
@@ -348,6 +357,23 @@ def run_gpu(args):
            "seconds_per_step": e2e_s,
            "step": f"pm_solve_tensor, {e2e_iters} iterations per rotated problem, host geometry "
                    "in, host tensor out"}
+    if not args.no_fp64:
+        # the same call for the plain FP64 form (the reference's precision)
+        t64 = []
+        for i in range(2):
+            barrier()
+            t0 = time.perf_counter()
+            K64, _ = pm.solve_tensor(g, None, max_iter=e2e_iters, precision="fp64", **common)
+            t1 = time.perf_counter()
+            if i >= 1:
+                t64.append(t1 - t0)
+        s64 = max_over_ranks(statistics.mean(t64))
+        forms["fp64"]["e2e"] = {"value": world * 3 * e2e_iters * nvox / s64 / 1e9,
+                                "unit": "GLUP/s", "seconds_per_step": s64,
+                                "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
+                                "d2h_bytes_per_step": e2e["d2h_bytes_per_step"],
+                                "tensor_rel_diff_vs_mixed":
+                                    float(np.abs(K64 - K).max() / np.abs(np.diag(K64)).max())}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -371,8 +397,87 @@ def run_gpu(args):
         if k_rel is not None:
             out["k_rel_diff_vs_fp64"] = k_rel
             out["k_rel_diff_vs_fp64_components"] = k_rel_components
+        if world == 1 and not args.no_serving:
+            # the serving target: batched mixed vs plain FP64 solves/h on the
+            # uneven stream, and latency percentiles on a request stream
+            out["c4"] = c4_result(args.c4_samples)
+            out["c5"] = c5_result(args.c5_requests, args.c5_max_axis)
         print(json.dumps(out), flush=True)
     rep.close()
+    return 0
+
+
+def kernel_traffic(kid, brick, size, nvox):
+    """DRAM bytes per launch of the chosen correction sweep from its committed
+    ncu capture (profiles/*_traffic.json), only when that capture is of the
+    same kernel id and fluid-list order and of the kernel sources as they are
+    now (their SHA-256 is recorded at capture time); otherwise None, with the
+    reason."""
+    import hashlib
+
+    tpath = os.path.join(ROOT, "profiles", f"{KERNELS[kid][0]}_sphere{size}_traffic.json")
+    if not os.path.exists(tpath):
+        return None, f"no ncu capture of {KERNELS[kid][0]} on this workload"
+    t = json.load(open(tpath))
+    if t.get("kernel_id") != kid or list(t.get("brick", [])) != list(brick):
+        return None, (f"capture is of kernel {t.get('kernel_id')} brick {t.get('brick')}, "
+                      f"the autotuner chose {kid} brick {brick}")
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update(open(os.path.join(ROOT, f), "rb").read())
+    if t.get("sources") != KERNEL_SOURCES or h.hexdigest() != t.get("sources_sha256"):
+        return None, "kernel sources changed since the capture"
+    return t["dram_bytes_per_launch"] * nvox / t["nvox"], t["source"]
+
+
+# Sources of each correction-sweep kernel: a traffic capture is valid while
+# their SHA-256 is the one recorded with it.
+KERNEL_SOURCES = ["poremaps_gb300/csrc/pm_fast.cu", "poremaps_gb300/csrc/pm_compact.cu",
+                  "poremaps_gb300/csrc/pm_stencil.cuh", "poremaps_gb300/csrc/pm_internal.h"]
+
+
+def write_traffic(csv_path, kid, brick, size):
+    """Turn an ncu CSV of the chosen correction sweep (the metrics
+    dram__bytes_read.sum and dram__bytes_write.sum, launches of
+    `bench.py --profile-case mixed --kernel K --brick ...`) into
+    profiles/<kernel>_sphere<size>_traffic.json, keyed to the kernel id, the
+    list order and the SHA-256 of the kernel sources."""
+    import csv
+    import hashlib
+
+    per = {}
+    with open(csv_path) as f:
+        rows = [r for r in csv.reader(f) if len(r) > 10]
+    head = rows[0]
+    ci = {n: head.index(n) for n in ("ID", "Kernel Name", "Metric Name", "Metric Unit",
+                                     "Metric Value")}
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    kshort = KERNELS[kid][0]
+    for r in rows[1:]:
+        if kshort not in r[ci["Kernel Name"]]:
+            continue
+        m = r[ci["Metric Name"]]
+        if m in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            v = float(r[ci["Metric Value"]].replace(",", "")) * scale[r[ci["Metric Unit"]]]
+            per[r[ci["ID"]]] = per.get(r[ci["ID"]], 0.0) + v
+    if not per:
+        raise SystemExit(f"no {kshort} launches with DRAM metrics in {csv_path}")
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update(open(os.path.join(ROOT, f), "rb").read())
+    out = {"kernel": kshort, "kernel_id": kid, "brick": list(brick),
+           "workload": f"{size}^3 sphere pack (bench default), mixed, one rotated problem",
+           "nvox": size ** 3, "dram_bytes_per_launch": statistics.mean(per.values()),
+           "launches": len(per), "sources": KERNEL_SOURCES, "sources_sha256": h.hexdigest(),
+           "source": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum "
+                     f"--clock-control none -k regex:{kshort} -s 5 -c 2 python bench.py "
+                     f"--profile-case mixed --kernel {kid} --brick {' '.join(map(str, brick))}; "
+                     "mean over the captured launches, cold caches, the bench's problem size"}
+    path = os.path.join(ROOT, "profiles", f"{kshort}_sphere{size}_traffic.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    print(json.dumps(out))
     return 0
 
 
@@ -383,7 +488,11 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
            4: ("k_brick_inner", "TMA brick tiles, FP32 correction sweep"),
            5: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 4 blocks/SM"),
            6: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 3 blocks/SM"),
-           7: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 2 blocks/SM")}
+           7: ("k_dc_inner_pf", "persistent fluid-list FP32 correction sweep, 2 blocks/SM"),
+           8: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
+                               "3 blocks/SM"),
+           9: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
+                               "4 blocks/SM")}
 
 
 def run_profile_case(args):
@@ -492,12 +601,19 @@ def k_errors(pairs):
                  "numerically_zero_k": {"threshold_m2": K_ZERO, "samples": zero}}
 
 
-def run_c4(args):
+def unconverged(results):
+    """Indices of the requests that reached max_iter without meeting the stop
+    rule: they count neither as solves nor in the latency percentiles."""
+    return [i for i, r in enumerate(results) if not r.converged]
+
+
+def c4_result(n_samples: int):
+    """The batched uneven stream (configuration 4) through the mixed-precision
+    server against the plain FP64 form solving the samples one by one."""
     import poremaps_gb300 as pm
 
-    pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     t_gen = time.perf_counter()
-    reqs = c4_samples(args.samples)
+    reqs = c4_samples(n_samples)
     t_gen = time.perf_counter() - t_gen
     nvox = sum(g.size for g, _ in reqs)
     # batched mixed-precision server
@@ -522,6 +638,8 @@ def run_c4(args):
             plain.append(p.solve())
     t_64 = time.perf_counter() - t0
     rel, kerr = k_errors([(done[i].result, r) for i, r in enumerate(plain)])
+    unc_mx = unconverged([done[i].result for i in range(len(reqs))])
+    unc_64 = unconverged(plain)
     out = {"metric": "solves/h", "value": 3600.0 * len(reqs) / t_mx, "unit": "solves/h",
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
            "config": {"workload": f"{len(reqs)} uneven samples (axes from {{32,48,64,96,128}}), "
@@ -529,8 +647,13 @@ def run_c4(args):
                                   "porosity U[0.15,0.5], bc 0/1, GS, eps 1e-6",
                       "total_voxels": nvox, "generation_s": t_gen},
            "batched_mixed": {"solves_per_h": 3600.0 * len(reqs) / t_mx, "seconds": t_mx,
+                             "converged_solves_per_h":
+                                 3600.0 * (len(reqs) - len(unc_mx)) / t_mx,
+                             "unconverged_at_max_iter": unc_mx,
                              "device_busy_ms": busy, "glups_busy": lups / (busy * 1e6)},
-           "plain_fp64": {"solves_per_h": 3600.0 * len(reqs) / t_64, "seconds": t_64},
+           "plain_fp64": {"solves_per_h": 3600.0 * len(reqs) / t_64, "seconds": t_64,
+                          "converged_solves_per_h": 3600.0 * (len(reqs) - len(unc_64)) / t_64,
+                          "unconverged_at_max_iter": unc_64},
            "speedup_vs_plain_fp64": t_64 / t_mx,
            "k_rel_err_vs_plain_fp64": kerr,
            "iterations": {"min": min(c.result.sweeps for c in done.values()),
@@ -546,15 +669,31 @@ def run_c4(args):
                    "converged": bool(done[i].result.converged), "wk33": done[i].result.wk33},
          "fp64": {"iterations": plain[i].iterations, "converged": bool(plain[i].converged),
                   "wk33": plain[i].wk33}} for i in order[:5]]
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
-def run_c5(args):
+def run_c4(args):
     import poremaps_gb300 as pm
 
     pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    reqs = c5_samples(args.samples, args.max_axis)
+    print(json.dumps(c4_result(args.samples)), flush=True)
+    return 0
+
+
+def pcts(lat, skip=()):
+    keep = np.array([x for i, x in enumerate(lat) if i not in set(skip)])
+    if keep.size == 0:
+        return {"p50_s": None, "p99_s": None}
+    return {"p50_s": float(np.percentile(keep, 50)), "p99_s": float(np.percentile(keep, 99))}
+
+
+def c5_result(n_requests: int, max_axis: int):
+    """A serving stream (configuration 5): Poisson arrivals through the
+    mixed-precision server, and the plain FP64 form serving the same arrivals
+    one request at a time."""
+    import poremaps_gb300 as pm
+
+    reqs = c5_samples(n_requests, max_axis)
     # arrival rate: keep the device busy -- mean inter-arrival = 0.6 x the mean
     # solve time estimated from the first request alone (scaled by voxels)
     rng = np.random.default_rng(55)
@@ -583,7 +722,7 @@ def run_c5(args):
     total = time.perf_counter() - t0
     busy, wall, lups = srv.stats()
     srv.close()
-    lat = np.array([c.finish_ms - c.submit_ms for c in done.values()]) / 1e3
+    lat = np.array([done[i].finish_ms - done[i].submit_ms for i in range(len(reqs))]) / 1e3
     # the plain FP64 GPU form on the same arrivals: one request at a time,
     # first come first served; each service time is a real solve on the GPU
     # (host geometry in, result out), the queueing follows from the arrivals
@@ -602,18 +741,27 @@ def run_c5(args):
         fp64_objs.append(r)
     rel, kerr = k_errors([(done[i].result, r) for i, r in enumerate(fp64_objs)])
     lat64 = np.array(lat64)
+    unc_mx = unconverged([done[i].result for i in range(len(reqs))])
+    unc_64 = unconverged(fp64_objs)
+    span64 = free_at - arrive[0]
     out = {"metric": "p99 time-to-permeability", "value": float(np.percentile(lat, 99)),
            "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f32+f64",
            "data": "synthetic",
            "config": {"workload": f"{len(reqs)} requests, Poisson arrivals, axes log-uniform in "
-                                  f"[32,{args.max_axis}], porosity U[0.12,0.45], bc 0/1/2, GS, "
+                                  f"[32,{max_axis}], porosity U[0.12,0.45], bc 0/1/2, GS, "
                                   "eps 1e-6, mixed-precision server"},
            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "converged_only": pcts(lat, unc_mx),
            "solves_per_h": 3600.0 * len(reqs) / total,
+           "converged_solves_per_h": 3600.0 * (len(reqs) - len(unc_mx)) / total,
+           "unconverged_at_max_iter": unc_mx,
            "device_busy_frac": (busy / 1e3) / total,
            "plain_fp64": {"p50_s": float(np.percentile(lat64, 50)),
                           "p99_s": float(np.percentile(lat64, 99)),
-                          "solves_per_h": 3600.0 * len(reqs) / (free_at - arrive[0]),
+                          "converged_only": pcts(lat64, unc_64),
+                          "solves_per_h": 3600.0 * len(reqs) / span64,
+                          "converged_solves_per_h": 3600.0 * (len(reqs) - len(unc_64)) / span64,
+                          "unconverged_at_max_iter": unc_64,
                           "service": "one request at a time, FIFO, same arrivals"},
            "k_rel_err_vs_plain_fp64": kerr,
            "failed": [{"index": i, "status": done[i].status} for i in range(len(reqs))
@@ -627,7 +775,14 @@ def run_c5(args):
                    "converged": bool(done[i].result.converged),
                    "k": [done[i].result.wk13, done[i].result.wk23, done[i].result.wk33]},
          "fp64": fp64_res[i]} for i in order[:4]]
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_c5(args):
+    import poremaps_gb300 as pm
+
+    pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps(c5_result(args.samples, args.max_axis)), flush=True)
     return 0
 
 
@@ -714,6 +869,8 @@ def run_c3(args):
 
 def main():
     args = parse()
+    if args.write_traffic:
+        return write_traffic(args.write_traffic, args.kernel, args.brick, args.size)
     if args.profile_case:
         return run_profile_case(args)
     if args.workload == "c3":

@@ -47,7 +47,8 @@ typedef enum {
   PM_ERR_NOMEM = 4,     /* device or host allocation failed / over budget */
   PM_ERR_NONFINITE = 5, /* NaN/Inf detected in a reduction */
   PM_ERR_BUSY = 6,      /* server full / request not finished */
-  PM_ERR_NOT_FOUND = 7
+  PM_ERR_NOT_FOUND = 7,
+  PM_ERR_CANCELLED = 8  /* server request withdrawn by pm_server_cancel */
 } pm_status;
 
 /* sweep ordering on the device */
@@ -96,14 +97,18 @@ typedef struct {
   int write_log;                /* 1: append the reference log rows to log_file_name */
   int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
   int kernel;                   /* correction sweep of the mixed form: -1 autotune
-                                   (default: time the fluid-list kernels 6, 5, 7, 2 on
-                                   the problem, keep the fastest),
+                                   (default: time the kernels 9, 8, 6, 5, 7, 2 on the
+                                   problem, keep the fastest),
                                    0 TMA z-march 32x16 tiles, 3 TMA
                                    z-march 32x8 tiles, 1 fluid-list gather, 2 fluid-list
                                    gather at four blocks per SM, 4 TMA bricks (one
                                    brick + halo per CTA in shared memory), 5 / 6 / 7
                                    persistent fluid-list gather, list prefetched, at
-                                   four / three / two blocks per SM */
+                                   four / three / two blocks per SM, 8 / 9 persistent
+                                   sweep over a compact store (correction and
+                                   residual of fluid voxels only, in fluid-list
+                                   order, six neighbour positions per voxel) at
+                                   three / four blocks per SM */
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */
@@ -243,10 +248,19 @@ uint64_t pm_kernel_launches(void);
  * library until exit); larger sizes return PM_ERR_INVALID.  All calls share that
  * array, so calls that overlap on the GPU race.  The first call on a device
  * looks up the array's address with that device current; make it before any
- * stream capture. */
+ * stream capture.  The address is kept for the life of the process: do not
+ * call this after cudaDeviceReset on that device.  The fluid-voxel counts that
+ * turn the sums into permeabilities (all fluid voxels, those in the box and on
+ * its zmin / zmax planes; evaluation.cc:192-210) are not returned: the caller
+ * counts them from its geometry. */
 pm_status pm_reduce_fields_noalloc(const int size[3], const uint8_t* geom, const double* u,
                                    const double* v, const double* w, const double* p,
                                    const int dom_interest[6], double* sums, void* stream);
+
+/* Device bytes pm_problem_create will hold for these parameters (fields,
+ * lists, codes, scratch): the footprint the server admits requests by.  No
+ * counterpart in the reference. */
+pm_status pm_problem_footprint(const pm_params* p, size_t* bytes);
 
 /* ---- batched / serving form: many uneven samples resident at once ---- */
 typedef struct {
@@ -255,6 +269,12 @@ typedef struct {
   int precision;            /* pm_precision for all requests */
   int use_graphs;           /* capture each it_eval block of sweeps in a CUDA graph */
   int autotune;             /* pick tile shapes per size class by timing */
+  int max_bypass;           /* backfill: when the request at the head of the queue does
+                               not fit the free budget, later requests that fit are
+                               admitted past it, at most max_bypass times before the
+                               head is admitted (0 = 64; negative = strict first come,
+                               first served).  A request larger than the whole budget
+                               completes at once with PM_ERR_NOMEM. */
 } pm_server_config;
 
 typedef struct pm_server pm_server;
@@ -278,6 +298,23 @@ pm_status pm_server_step(pm_server* s, int* active);
 pm_status pm_server_poll(pm_server* s, pm_completion* out, int max, int* n);
 pm_status pm_server_stats(pm_server* s, double* busy_ms, double* wall_ms, uint64_t* lups);
 double pm_server_clock_ms(pm_server* s);
+/* Withdraw a request: a queued one is removed, a resident one is retired at
+ * once (between scheduling rounds; its device memory is freed and the others
+ * continue).  Either way its completion carries PM_ERR_CANCELLED and no
+ * result.  PM_ERR_NOT_FOUND when the ticket has already completed or was never
+ * issued.  No counterpart in the reference (one run per process). */
+pm_status pm_server_cancel(pm_server* s, uint64_t ticket);
+/* Device bytes the server would admit this request by (its footprint with the
+ * server's precision and kernels), to plan budgets.  No counterpart in the
+ * reference. */
+pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* bytes);
+
+/* ---- test hook (no counterpart in the reference) ----
+ * Makes the nth device allocation of problem set-up from now on (1 = the next
+ * one) fail as an out-of-memory error would, so that callers can exercise
+ * their PM_ERR_NOMEM handling on the host without exhausting a GPU; 0 clears
+ * it.  Process-wide. */
+pm_status pm_debug_fail_alloc(int nth);
 
 #ifdef __cplusplus
 }

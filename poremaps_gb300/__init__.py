@@ -32,7 +32,10 @@ PRECISIONS = {"fp64": 0, "mixed": 1}
 ARITHS = {"exact": 0, "fast": 1}
 
 STATUS = {0: "PM_OK", 1: "PM_ERR_INVALID", 2: "PM_ERR_IO", 3: "PM_ERR_CUDA", 4: "PM_ERR_NOMEM",
-          5: "PM_ERR_NONFINITE", 6: "PM_ERR_BUSY", 7: "PM_ERR_NOT_FOUND"}
+          5: "PM_ERR_NONFINITE", 6: "PM_ERR_BUSY", 7: "PM_ERR_NOT_FOUND", 8: "PM_ERR_CANCELLED"}
+PM_ERR_NOMEM = 4
+PM_ERR_NOT_FOUND = 7
+PM_ERR_CANCELLED = 8
 
 
 class PMError(RuntimeError):
@@ -67,7 +70,8 @@ class Result(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int),
-                ("precision", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int)]
+                ("precision", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
+                ("max_bypass", C.c_int)]
 
 
 class Completion(C.Structure):
@@ -85,7 +89,8 @@ EXPORTS = ["pm_last_error", "pm_last_error_copy", "pm_version", "pm_params_defau
            "pm_block_timed", "pm_block_group_timed", "pm_kernel_time", "pm_kernel_launches", "pm_get_kernel", "pm_get_brick", "pm_reduce_fields_noalloc",
            "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
-           "pm_server_clock_ms"]
+           "pm_server_clock_ms", "pm_server_cancel", "pm_debug_fail_alloc",
+           "pm_problem_footprint", "pm_server_request_bytes"]
 
 _lib = None
 
@@ -142,6 +147,10 @@ def load_library(path: str = LIB_PATH):
         "pm_server_poll": (C.c_int, [vp, P(Completion), C.c_int, P(C.c_int)]),
         "pm_server_stats": (C.c_int, [vp, P(C.c_double), P(C.c_double), P(C.c_uint64)]),
         "pm_server_clock_ms": (C.c_double, [vp]),
+        "pm_server_cancel": (C.c_int, [vp, C.c_uint64]),
+        "pm_debug_fail_alloc": (C.c_int, [C.c_int]),
+        "pm_problem_footprint": (C.c_int, [P(Params), P(C.c_size_t)]),
+        "pm_server_request_bytes": (C.c_int, [vp, P(Params), P(C.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):
@@ -150,6 +159,23 @@ def load_library(path: str = LIB_PATH):
             f.argtypes = args
     _lib = L
     return L
+
+
+def footprint(shape, **kw) -> int:
+    """pm_problem_footprint: device bytes of a problem of this (nz, ny, nx)
+    shape and these parameters."""
+    nz, ny, nx = shape
+    p = default_params(**kw)
+    p.size[0], p.size[1], p.size[2] = nx, ny, nz
+    b = C.c_size_t()
+    _check(load_library().pm_problem_footprint(C.byref(p), C.byref(b)))
+    return b.value
+
+
+def debug_fail_alloc(nth: int) -> None:
+    """pm_debug_fail_alloc: the nth device allocation of problem set-up from
+    now on fails as out of memory (0 clears)."""
+    _check(load_library().pm_debug_fail_alloc(int(nth)))
 
 
 def _check(st: int):
@@ -355,9 +381,11 @@ class Server:
     """Batched / continuously batching solver (pm_server_* of the C ABI)."""
 
     def __init__(self, precision: str | int = "mixed", hbm_budget_bytes: int = 0,
-                 max_resident: int = 0, use_graphs: int = 1, autotune: int = 0):
+                 max_resident: int = 0, use_graphs: int = 1, autotune: int = 0,
+                 max_bypass: int = 0):
         cfg = ServerConfig(hbm_budget_bytes, max_resident,
-                           PRECISIONS.get(precision, precision), use_graphs, autotune)
+                           PRECISIONS.get(precision, precision), use_graphs, autotune,
+                           max_bypass)
         self.h = C.c_void_p()
         _check(load_library().pm_server_create(C.byref(cfg), C.byref(self.h)))
 
@@ -388,6 +416,27 @@ class Server:
 
     def clock_ms(self) -> float:
         return load_library().pm_server_clock_ms(self.h)
+
+    def request_bytes(self, geom: np.ndarray, **kw) -> int:
+        """pm_server_request_bytes: the footprint this server admits the
+        request by."""
+        nz, ny, nx = geom.shape
+        p = default_params(**kw)
+        p.size[0], p.size[1], p.size[2] = nx, ny, nz
+        b = C.c_size_t()
+        _check(load_library().pm_server_request_bytes(self.h, C.byref(p), C.byref(b)))
+        return b.value
+
+    def cancel(self, ticket: int) -> int:
+        """pm_server_cancel: returns the status (0, or PM_ERR_NOT_FOUND when the
+        ticket has already completed)."""
+        return load_library().pm_server_cancel(self.h, C.c_uint64(ticket))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def close(self):
         if self.h:

@@ -29,6 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = [
     ("pm_kernels.cu", ["-fmad=false"]),
     ("pm_fast.cu", []),
+    ("pm_compact.cu", []),
     ("pm_zmarch.cu", []),
     ("pm_brick.cu", []),
     ("pm_api.cpp", []),

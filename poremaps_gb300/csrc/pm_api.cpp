@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <chrono>
 #include <map>
@@ -22,6 +23,7 @@
 
 #include "../../include/poremaps.h"
 #include "pm_api_internal.h"
+#include "pm_compact.h"
 #include "pm_internal.h"
 
 using namespace pm;
@@ -42,6 +44,22 @@ pm_status set_error(pm_status st, const char* fmt, ...) {
   va_end(ap);
   g_err = buf;
   return st;
+}
+
+// Countdown of pm_debug_fail_alloc: the allocation that takes it from 1 to 0
+// fails as cudaMalloc does when the device is out of memory.
+std::atomic<int> g_fail_alloc{0};
+
+template <typename T>
+cudaError_t dev_alloc(T** ptr, size_t bytes) {
+  int n = g_fail_alloc.load();
+  while (n > 0 && !g_fail_alloc.compare_exchange_weak(n, n - 1)) {
+  }
+  if (n == 1) {
+    *ptr = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc((void**)ptr, bytes);
 }
 
 pm_status cuda_error(cudaError_t e, const char* where) {
@@ -85,7 +103,7 @@ pm_status validate(const pm_params* p) {
     if (!none && !all)
       return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
   }
-  if (p->kernel < -1 || p->kernel > 7) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel < -1 || p->kernel > 9) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
   if (p->kernel == 4 && p->brick[0] && pm::brick_shape_of(p->brick[0], p->brick[1], p->brick[2]) < 0)
     return set_error(PM_ERR_INVALID, "kernel 4 bricks are 32x8x8, 32x8x4 or 32x4x4");
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
@@ -115,7 +133,10 @@ pm_status device_sync(pm_problem* pr, const char* where) {
 
 // The FP32 correction sweep e_out = L(e_in) + r of the mixed form.
 pm_status correction_sweep(pm_problem* pr, int src) {
-  if (pr->zp) {
+  if (pr->compact()) {
+    CK(launch_dc_inner_c(pr->Ec[src], pr->Ec[1 - src], pr->Rc, pr->cmeta, pr->cslot4,
+                         pr->cslot2, pr->nlist, pr->solver, pr->kern == 8 ? 3 : 4, pr->st));
+  } else if (pr->zp) {
     CK(zmarch_inner(pr->zp, src, pr->E[1 - src], pr->g, pr->solver, pr->st));
   } else if (pr->bp) {
     CK(brick_inner(pr->bp, src, pr->E[1 - src], pr->R, pr->list, pr->g, pr->solver, pr->st));
@@ -200,22 +221,61 @@ pm_status choose_fp64_shapes(pm_problem* pr) {
 // gather compiled for four blocks per SM, 4 TMA bricks (32x8x8, 32x8x4 or
 // 32x4x4 voxels per CTA, the fluid list in the same brick order), 5,
 // 6 and 7 persistent fluid-list gather with the list prefetched (4 / 3 / 2
-// CTAs per SM).
+// CTAs per SM), 8 and 9 persistent sweep over the compact store
+// (pm_compact.cu: fluid voxels only, six precomputed neighbour positions per
+// voxel; 3 / 4 CTAs per SM).
 // kernel < 0 times the fluid-list candidates on this problem (a few launches
 // each; the correction buffers are scratch until the first residual sweep)
 // and keeps the fastest.
+pm_status zero_corrections(pm_problem* pr) {
+  if (pr->E[0]) {
+    CK(launch_zero4(pr->E[0], pr->g, pr->st));
+    CK(launch_zero4(pr->E[1], pr->g, pr->st));
+  }
+  if (pr->Ec[0])
+    CK(cudaMemsetAsync(pr->c_base, 0, 2 * sizeof(float4) * ((size_t)pr->nlist + 1), pr->st));
+  return PM_OK;
+}
+
+// Frees the correction store the chosen kernel does not use.
+void release_unused_store(pm_problem* pr) {
+  if (pr->compact()) {
+    cudaFree(pr->f32_base);
+    pr->f32_base = nullptr;
+    pr->E[0] = pr->E[1] = pr->R = nullptr;
+  } else {
+    cudaFree(pr->c_base);
+    cudaFree(pr->cslot4);
+    cudaFree(pr->cslot2);
+    cudaFree(pr->cmeta);
+    cudaFree(pr->cwords);
+    pr->c_base = pr->Ec[0] = pr->Ec[1] = pr->Rc = nullptr;
+    pr->cslot4 = nullptr;
+    pr->cslot2 = nullptr;
+    pr->cmeta = nullptr;
+    pr->cwords = nullptr;
+  }
+}
+
 pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   const bool tma = zmarch_available() != 0;
-  // set up kernel k with the fluid list in brick order b (k 1, 2, 4)
+  static const int kLex[3] = {0, 0, 0};
+  // set up kernel k with the fluid list in brick order b (k 1, 2, 4); the
+  // compact store (k 8) needs the lexicographic list
   auto make = [&](int k, const int* b) -> pm_status {
     if (pr->zp) { zmarch_destroy(pr->zp); pr->zp = nullptr; }
     if (pr->bp) { brick_destroy(pr->bp); pr->bp = nullptr; }
     pr->kern = k;
+    const bool cpt = k == 8 || k == 9;
+    if (cpt) b = kLex;
     {
       int* dcount = (int*)pr->dout;
       CK(launch_fluid_list(pr->codes, pr->g, pr->list, dcount, pr->st, b[0], b[1], b[2]));
       for (int i = 0; i < 3; ++i) pr->brick[i] = b[i];
     }
+    if (cpt)
+      CK(compact_setup(pr->codes, pr->g, pr->list, pr->nlist, pr->cwords, pr->cslot4,
+                       pr->cslot2, pr->cmeta, pr->st));
     if (k == 0 || k == 3)
       CK(zmarch_create(&pr->zp, pr->g, pr->E[0], pr->E[1], pr->R, pr->codes, 0, k == 3));
     if (k == 4)
@@ -223,7 +283,6 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
                       brick_shape_of(b[0], b[1], b[2]), pr->st));
     return PM_OK;
   };
-  static const int kLex[3] = {0, 0, 0};
   if (kernel >= 0) {
     if ((kernel == 0 || kernel == 3 || kernel == 4) && !tma) kernel = 1;
     const int* b = pr->prm.brick;
@@ -250,18 +309,19 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   if (hit != tuned.end()) {
     pm_status s = make(hit->second.k, hit->second.b);
     if (s != PM_OK) return s;
+    release_unused_store(pr);
     return device_sync(pr, "kernel choice");
   }
   // The TMA kernels (0, 3, 4) lose on every medium measured so far and are
   // left to explicit choice; timing them would only lengthen the set-up of
   // every problem.
-  const Cand cands[] = {{6, {0, 0, 0}}, {6, {32, 8, 8}}, {5, {0, 0, 0}}, {7, {0, 0, 0}},
-                        {2, {0, 0, 0}}};
-  const int nc = 5;
+  const Cand cands[] = {{9, {0, 0, 0}}, {8, {0, 0, 0}}, {6, {0, 0, 0}}, {6, {32, 8, 8}},
+                        {5, {0, 0, 0}}, {7, {0, 0, 0}}, {2, {0, 0, 0}}};
+  const int nc = 7;
   // Each candidate: the best of three timings of five sweeps.  The first
   // candidate is kept unless another one is at least 2 % faster, so timing
   // noise does not flip the choice between near-equal kernels.
-  float t[5];
+  float t[nc];
   for (int i = 0; i < nc; ++i) {
     pm_status s;
     if ((s = make(cands[i].k, cands[i].b)) != PM_OK) return s;
@@ -286,9 +346,10 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   tuned[key] = cands[bi];
   pm_status s = make(cands[bi].k, cands[bi].b);
   if (s != PM_OK) return s;
-  CK(launch_zero4(pr->E[0], pr->g, pr->st));
-  CK(launch_zero4(pr->E[1], pr->g, pr->st));
-  return device_sync(pr, "kernel autotune");
+  if ((s = zero_corrections(pr)) != PM_OK) return s;
+  if ((s = device_sync(pr, "kernel autotune")) != PM_OK) return s;
+  release_unused_store(pr);
+  return PM_OK;
 }
 
 // Block size of the reference-order wavefront, timed on the problem: a few
@@ -331,8 +392,12 @@ pm_status choose_wavefront_shape(pm_problem* pr) {
 
 pm_status dc_flush(pm_problem* pr) {
   if (pr->dc_pos > 0) {
-    CK(launch_dc_correct_list(pr->F[pr->cur], pr->E[pr->ecur], pr->list, pr->nlist, pr->g,
-                              pr->st));
+    if (pr->compact())
+      CK(launch_dc_correct_c(pr->F[pr->cur], pr->Ec[pr->ecur], pr->list, pr->nlist, pr->g,
+                             pr->st));
+    else
+      CK(launch_dc_correct_list(pr->F[pr->cur], pr->E[pr->ecur], pr->list, pr->nlist, pr->g,
+                                pr->st));
     pr->dc_pos = 0;
   }
   return PM_OK;
@@ -346,8 +411,12 @@ namespace {
 
 pm_status iterate_mixed(pm_problem* pr) {
   if (pr->dc_pos == 0) {
-    CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list, pr->nlist,
-                          pr->g, pr->solver, pr->st));
+    if (pr->compact())
+      CK(launch_dc_residual_c(pr->F[pr->cur], pr->Rc, pr->Ec[pr->ecur], pr->codes, pr->list,
+                              pr->nlist, pr->g, pr->solver, pr->st));
+    else
+      CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list,
+                            pr->nlist, pr->g, pr->solver, pr->st));
   } else {
     pm_status s = correction_sweep(pr, pr->ecur);
     if (s != PM_OK) return s;
@@ -454,13 +523,15 @@ pm_status reduce_launch(pm_problem* pr, int full) {
                        pr->st));
     return PM_OK;
   }
+  const bool cpt = pr->compact();
+  const float4* e = cpt ? pr->Ec[pr->ecur] : pr->E[pr->ecur];
   if (!full) {
-    CK(launch_reduce_check(pr->F[pr->cur], pr->E[pr->ecur], mode, pr->list, pr->nlist, pr->g,
-                           pr->partials, pr->dout, pr->st));
+    CK(launch_reduce_check(pr->F[pr->cur], e, mode, pr->list, pr->nlist, pr->g, pr->partials,
+                           pr->dout, pr->st, cpt));
   } else {
-    CK(launch_reduce(pr->F[pr->cur], pr->E[pr->ecur], mode, full,
-                     pr->order != PM_ORDER_REFERENCE, pr->codes, pr->g,
-                     pr->prm.dom_interest, pr->partials, pr->dout, pr->st));
+    CK(launch_reduce(pr->F[pr->cur], e, mode, full, pr->order != PM_ORDER_REFERENCE, pr->codes,
+                     pr->g, pr->prm.dom_interest, pr->partials, pr->dout, pr->st,
+                     cpt ? pr->cwords : nullptr));
   }
   CK(cudaMemcpyAsync(pr->hout, pr->dout, sizeof(double) * kRedVals, cudaMemcpyDeviceToHost,
                      pr->st));
@@ -482,8 +553,8 @@ pm_status reset_state(pm_problem* pr) {
   CK(launch_init64(pr->F[0], pr->codes, pr->g, pr->st));
   CK(launch_copy_fields64(pr->F[1], pr->F[0], pr->g, pr->st));
   if (pr->precision == PM_PREC_MIXED) {
-    CK(launch_zero4(pr->E[0], pr->g, pr->st));
-    CK(launch_zero4(pr->E[1], pr->g, pr->st));
+    pm_status s = zero_corrections(pr);
+    if (s != PM_OK) return s;
   }
   pr->cur = pr->ecur = pr->dc_pos = 0;
   pr->iteration = 0;
@@ -561,7 +632,14 @@ pm_status write_log_row(const char* path, bool first, int iteration, double conv
 size_t problem_device_bytes(const pm_params* p) {
   Grid g = make_grid(p->size[0], p->size[1], p->size[2], p->boundary_method);
   size_t b = (size_t)g.allocc + 4 * (size_t)g.nvox + 2 * 4 * 8 * (size_t)g.alloc64;
-  if (p->precision == PM_PREC_MIXED) b += 3 * sizeof(float4) * (size_t)g.alloc4;
+  // the padded correction store, the compact one (fluid voxels <= voxels), or
+  // both while the autotuner times kernels of either
+  const bool cpt = p->kernel == 8 || p->kernel == 9;
+  if (p->precision == PM_PREC_MIXED && !cpt) b += 3 * sizeof(float4) * (size_t)g.alloc4;
+  if (p->precision == PM_PREC_MIXED && (cpt || p->kernel < 0))
+    b += (3 * sizeof(float4) + sizeof(int4) + sizeof(int2) + sizeof(uint16_t)) *
+             ((size_t)g.nvox + 1) +
+         sizeof(uint2) * (size_t)compact_words(g);
   b += 8 * (size_t)g.nvox;  // export scratch
   return b + (1 << 20);
 }
@@ -582,6 +660,20 @@ size_t pm_last_error_copy(char* buf, size_t size) {
   return n;
 }
 const char* pm_version(void) { return "poremaps_gb300 0.1 (sm_103a)"; }
+
+pm_status pm_problem_footprint(const pm_params* p, size_t* bytes) {
+  if (!bytes) return set_error(PM_ERR_INVALID, "bytes is NULL");
+  pm_status s = validate(p);
+  if (s != PM_OK) return s;
+  *bytes = problem_device_bytes(p);
+  return PM_OK;
+}
+
+pm_status pm_debug_fail_alloc(int nth) {
+  if (nth < 0) return set_error(PM_ERR_INVALID, "nth must be >= 0");
+  g_fail_alloc.store(nth);
+  return PM_OK;
+}
 
 pm_status pm_params_default(pm_params* p) {
   if (!p) return set_error(PM_ERR_INVALID, "params is NULL");
@@ -639,18 +731,18 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   sm_count();  // device query outside any later graph capture
   CKF(cudaEventCreate(&pr->ev0));
   CKF(cudaEventCreate(&pr->ev1));
-  CKF(cudaMalloc((void**)&pr->codes_base, g.allocc));
+  CKF(dev_alloc((void**)&pr->codes_base, g.allocc));
   pr->codes = pr->codes_base + kXoffC;
   CKF(cudaMemsetAsync(pr->codes_base, 0, g.allocc, pr->st));
-  CKF(cudaMalloc((void**)&pr->list, sizeof(int) * (size_t)(g.nvox > 0 ? g.nvox : 1)));
+  CKF(dev_alloc((void**)&pr->list, sizeof(int) * (size_t)(g.nvox > 0 ? g.nvox : 1)));
   for (int b = 0; b < 2; ++b) {
-    CKF(cudaMalloc((void**)&pr->f64_base[b], 4 * sizeof(double) * (size_t)g.alloc64));
+    CKF(dev_alloc((void**)&pr->f64_base[b], 4 * sizeof(double) * (size_t)g.alloc64));
     double* base = pr->f64_base[b];
     pr->F[b] = {base + kXoff64, base + g.alloc64 + kXoff64, base + 2 * g.alloc64 + kXoff64,
                 base + 3 * g.alloc64 + kXoff64};
   }
-  if (pr->precision == PM_PREC_MIXED) {
-    CKF(cudaMalloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
+  if (pr->precision == PM_PREC_MIXED && p->kernel != 8 && p->kernel != 9) {
+    CKF(dev_alloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
     CKF(cudaMemsetAsync(pr->f32_base, 0, 3 * sizeof(float4) * (size_t)g.alloc4, pr->st));
     for (int k = 0; k < 3; ++k) {
       float4* f = pr->f32_base + k * g.alloc4 + kXoff4;
@@ -658,11 +750,11 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       else pr->R = f;
     }
   }
-  CKF(cudaMalloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
-  CKF(cudaMalloc((void**)&pr->dout, sizeof(double) * 16));
+  CKF(dev_alloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
+  CKF(dev_alloc((void**)&pr->dout, sizeof(double) * 16));
   CKF(cudaMallocHost((void**)&pr->hout, sizeof(double) * 16));
   pr->scratch_bytes = 8 * (size_t)g.nvox;
-  CKF(cudaMalloc(&pr->scratch, pr->scratch_bytes));
+  CKF(dev_alloc(&pr->scratch, pr->scratch_bytes));
   // geometry upload (through the export scratch) -> codes -> fluid list
   CKF(cudaMemcpyAsync(pr->scratch, geom, (size_t)g.nvox, cudaMemcpyHostToDevice, pr->st));
   CKF(launch_codes((const uint8_t*)pr->scratch, pr->codes, g, pr->st));
@@ -689,6 +781,18 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       return fail(set_error(PM_ERR_CUDA, "red-black fluid lists do not add up"));
   }
   if (pr->precision == PM_PREC_MIXED) {
+    if (p->kernel == 8 || p->kernel == 9 || p->kernel < 0) {
+      const size_t nl = (size_t)pr->nlist + 1;  // and the zero slot
+      CKF(dev_alloc((void**)&pr->c_base, 3 * sizeof(float4) * nl));
+      CKF(cudaMemsetAsync(pr->c_base, 0, 3 * sizeof(float4) * nl, pr->st));
+      pr->Ec[0] = pr->c_base;
+      pr->Ec[1] = pr->c_base + nl;
+      pr->Rc = pr->c_base + 2 * nl;
+      CKF(dev_alloc((void**)&pr->cslot4, sizeof(int4) * nl));
+      CKF(dev_alloc((void**)&pr->cslot2, sizeof(int2) * nl));
+      CKF(dev_alloc((void**)&pr->cmeta, sizeof(uint16_t) * nl));
+      CKF(dev_alloc((void**)&pr->cwords, sizeof(uint2) * (size_t)compact_words(g)));
+    }
     pm_status ts = choose_correction_kernel(pr, p->kernel);
     if (ts != PM_OK) return fail(ts);
   }
@@ -724,6 +828,11 @@ pm_status pm_problem_destroy(pm_problem* pr) {
   cudaFree(pr->f64_base[0]);
   cudaFree(pr->f64_base[1]);
   cudaFree(pr->f32_base);
+  cudaFree(pr->c_base);
+  cudaFree(pr->cslot4);
+  cudaFree(pr->cslot2);
+  cudaFree(pr->cmeta);
+  cudaFree(pr->cwords);
   cudaFree(pr->partials);
   cudaFree(pr->dout);
   if (pr->hout) cudaFreeHost(pr->hout);
@@ -909,8 +1018,12 @@ pm_status pm_kernel_time(pm_problem* pr, int kernel, int n, double* avg_ms) {
     if (pr->precision == PM_PREC_MIXED) {
       if (kernel == 1) {
         if (pr->dc_pos != 0) return set_error(PM_ERR_INVALID, "residual timing needs dc_pos 0");
-        CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list,
-                              pr->nlist, pr->g, pr->solver, pr->st));
+        if (pr->compact())
+          CK(launch_dc_residual_c(pr->F[pr->cur], pr->Rc, pr->Ec[pr->ecur], pr->codes, pr->list,
+                                  pr->nlist, pr->g, pr->solver, pr->st));
+        else
+          CK(launch_dc_residual(pr->F[pr->cur], pr->R, pr->E[pr->ecur], pr->codes, pr->list,
+                                pr->nlist, pr->g, pr->solver, pr->st));
       } else {
         pm_status s = correction_sweep(pr, pr->ecur);
         if (s != PM_OK) return s;

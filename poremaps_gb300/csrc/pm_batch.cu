@@ -6,8 +6,11 @@
 // full while small samples finish and new ones arrive.  Each voxel runs the
 // same device function as the single-problem kernels (pm_stencil.cuh), so a
 // sample's fields are identical whether it is solved alone or in a batch.
+// The mixed form's correction and residual are the compact store of
+// pm_compact.cu (one float4 per fluid-list position), as the single-problem
+// kernel 8 uses them.
 #include "pm_batch.h"
-#include "pm_stencil.cuh"
+#include "pm_compact.cuh"
 
 namespace pm {
 
@@ -38,7 +41,7 @@ __device__ __forceinline__ void walk_items(const SampleDesc* d, const WorkItem* 
     for (; q < w.count; q += blockDim.x) {
       const int qn = q + blockDim.x;
       const int next = qn < w.count ? __ldg(list + qn) : 0;
-      f(sd, lin);
+      f(sd, w.start + q, lin);
       lin = next;
     }
   }
@@ -48,12 +51,12 @@ __device__ __forceinline__ void walk_items(const SampleDesc* d, const WorkItem* 
 // (then each voxel dispatches on its sample's solver).
 template <int S>
 __global__ void k_batch_residual(const SampleDesc* d, const WorkItem* items, int nitems) {
-  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int q, int lin) {
     float4* E = sd.ecur0 ? sd.E1 : sd.E0;
     const int sv = S ? S : sd.solver;
-    if (sv == 3) dc_residual_voxel<3>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
-    else if (sv == 2) dc_residual_voxel<2>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
-    else dc_residual_voxel<1>(sd.X0, sd.R, E, sd.codes, sd.g, lin);
+    if (sv == 3) residual_c_voxel<3>(sd.X0, sd.R, E, sd.codes, sd.g, q, lin);
+    else if (sv == 2) residual_c_voxel<2>(sd.X0, sd.R, E, sd.codes, sd.g, q, lin);
+    else residual_c_voxel<1>(sd.X0, sd.R, E, sd.codes, sd.g, q, lin);
   });
 }
 
@@ -63,29 +66,29 @@ __global__ void k_batch_residual(const SampleDesc* d, const WorkItem* items, int
 template <int S>
 __global__ void __launch_bounds__(512, 2)
     k_batch_inner(const SampleDesc* d, const WorkItem* items, int nitems, int round) {
-  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int q, int lin) {
     const int a = (sd.ecur0 + round - 1) & 1;
     const float4* Ein = a ? sd.E1 : sd.E0;
     float4* Eout = a ? sd.E0 : sd.E1;
     const int sv = S ? S : sd.solver;
-    if (sv == 3) dc_inner_voxel<3>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
-    else if (sv == 2) dc_inner_voxel<2>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
-    else dc_inner_voxel<1>(Ein, Eout, sd.R, sd.codes, sd.g, lin);
+    if (sv == 3) inner_c_voxel<3>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, q);
+    else if (sv == 2) inner_c_voxel<2>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, q);
+    else inner_c_voxel<1>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, q);
   });
 }
 
 __global__ void k_batch_correct(const SampleDesc* d, const WorkItem* items, int nitems,
                                 int rounds) {
-  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int q, int lin) {
     const int a = (sd.ecur0 + rounds - 1) & 1;
-    dc_correct_voxel(sd.X0, a ? sd.E1 : sd.E0, sd.g, lin);
+    correct_c_voxel(sd.X0, __ldg((a ? sd.E1 : sd.E0) + q), sd.g, lin);
   });
 }
 
 template <int S>
 __global__ void k_batch_sweep64(const SampleDesc* d, const WorkItem* items, int nitems,
                                 int round) {
-  walk_items(d, items, nitems, [&](const SampleDesc& sd, int lin) {
+  walk_items(d, items, nitems, [&](const SampleDesc& sd, int, int lin) {
     const int a = (sd.xcur0 + round) & 1;
     const Fields<double>& A = a ? sd.X1 : sd.X0;
     const Fields<double>& B = a ? sd.X0 : sd.X1;

@@ -130,13 +130,17 @@ cudaError_t launch_zero4(float4* e, const Grid& g, cudaStream_t st);
 // implied3: the state stores swept pressure on the last interior plane and the
 // reapplied 3 is implied there (out-of-place orderings).
 // The convergence check's sum (value 2: sum of w, + e.z in mode 1) over the
-// fluid list; the other values of out are 0.
+// fluid list; the other values of out are 0.  compact: e is the compact store
+// (one float4 per list position) instead of the padded one.
 cudaError_t launch_reduce_check(Fields<double> x, const float4* e, int mode, const int* list,
                                 int nlist, const Grid& g, double* partials, double* out,
-                                cudaStream_t st);
+                                cudaStream_t st, int compact = 0);
+// words (non-null): e is the compact store, located through these fluid-mask
+// words (pm_compact.h).
 cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
                           const uint8_t* codes, const Grid& g, const int di[6],
-                          double* partials, double* out, cudaStream_t st);
+                          double* partials, double* out, cudaStream_t st,
+                          const uint2* words = nullptr);
 
 // The same sums in the reference's serial lexicographic order (bitwise equal
 // to the reference's reductions; used by the reference order).

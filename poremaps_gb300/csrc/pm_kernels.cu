@@ -69,11 +69,15 @@ Grid make_grid(int nx, int ny, int nz, int bm) {
 // its own neighbour), on non-periodic axes the halo is fluid (geometry halos
 // start at 0 and are never received, geometry.cc:98-106).
 __device__ __forceinline__ bool raw_solid(const uint8_t* raw, const Grid& g, int x, int y, int z) {
+  // An axis of length 1 has no image one period away for its outer halo
+  // cells: the reference's self-exchange copies a halo cell that still holds
+  // its initial fluid value there, so they are fluid too.
   auto fold = [](int c, int n, int per, bool& outside) {
     int i = c - 2;
     if (i < 0 || i >= n) {
       if (!per) { outside = true; return 0; }
       i = i < 0 ? i + n : i - n;
+      if (i < 0 || i >= n) { outside = true; return 0; }
     }
     return i;
   };
@@ -533,10 +537,10 @@ cudaError_t sweep64_exact(Fields<double> A, Fields<double> B, const uint8_t* cod
 // a fixed grid and a fixed combination tree (bitwise reproducible).
 template <int MODE>
 __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, const float4* e,
-                                                        int full, int implied3,
-                                                        const uint8_t* codes, Grid g,
-                                                        int d0, int d1, int d2, int d3, int d4,
-                                                        int d5, double* partials) {
+                                                        const uint2* words, int full,
+                                                        int implied3, const uint8_t* codes,
+                                                        Grid g, int d0, int d1, int d2, int d3,
+                                                        int d4, int d5, double* partials) {
   double acc[kRedVals];
   for (int i = 0; i < kRedVals; ++i) acc[i] = 0.0;
   const bool dofi = d0 | d1 | d2 | d3 | d4 | d5;
@@ -550,7 +554,15 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, const 
     long long c = (long long)Z * g.pl64 + (long long)Y * g.px64 + X;
     long long c4 = (long long)Z * g.pl4 + (long long)Y * g.px4 + X;
     float4 ev = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (MODE == 1) ev = e[c4];
+    if (MODE == 1) {
+      if (words) {  // compact store: the voxel's position in the fluid list
+        const int nw = (g.nx + 31) / 32;
+        const uint2 wd = words[r * nw + (xp >> 5)];
+        ev = e[(int)wd.y + __popc(wd.x & ((1u << (xp & 31)) - 1u))];
+      } else {
+        ev = e[c4];
+      }
+    }
     double w = x.w[c];
     if (MODE == 1) w += (double)ev.z;
     acc[2] += w;
@@ -590,14 +602,16 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(Fields<double> x, const 
 // order, fixed shuffle tree per warp, fixed order over the block's warps.
 template <int MODE>
 __global__ void __launch_bounds__(kRedThreads) k_reduce_check(Fields<double> x, const float4* e,
-                                                              const int* list, int nlist,
-                                                              Grid g, double* partials) {
+                                                              int compact, const int* list,
+                                                              int nlist, Grid g,
+                                                              double* partials) {
   double acc = 0.0;
   for (int q = blockIdx.x * kRedThreads + threadIdx.x; q < nlist; q += kRedBlocks * kRedThreads) {
     int X, Y, Z;
     lin_to_xyz(__ldg(list + q), g, X, Y, Z);
     double w = x.w[(long long)Z * g.pl64 + (long long)Y * g.px64 + X];
-    if (MODE == 1) w += (double)e[(long long)Z * g.pl4 + (long long)Y * g.px4 + X].z;
+    if (MODE == 1)
+      w += (double)e[compact ? (long long)q : (long long)Z * g.pl4 + (long long)Y * g.px4 + X].z;
     acc += w;
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -638,11 +652,13 @@ __global__ void __launch_bounds__(32 * kRedVals) k_reduce_final(const double* pa
 
 cudaError_t launch_reduce_check(Fields<double> x, const float4* e, int mode, const int* list,
                                 int nlist, const Grid& g, double* partials, double* out,
-                                cudaStream_t st) {
+                                cudaStream_t st, int compact) {
   if (mode == 0)
-    k_reduce_check<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, list, nlist, g, partials);
+    k_reduce_check<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, compact, list, nlist, g,
+                                                           partials);
   else
-    k_reduce_check<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, list, nlist, g, partials);
+    k_reduce_check<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, compact, list, nlist, g,
+                                                           partials);
   k_reduce_final<<<1, 32 * kRedVals, 0, st>>>(partials, out);
   count_launches(2);
   return cudaGetLastError();
@@ -650,13 +666,15 @@ cudaError_t launch_reduce_check(Fields<double> x, const float4* e, int mode, con
 
 cudaError_t launch_reduce(Fields<double> x, const float4* e, int mode, int full, int implied3,
                           const uint8_t* codes, const Grid& g, const int di[6], double* partials,
-                          double* out, cudaStream_t st) {
+                          double* out, cudaStream_t st, const uint2* words) {
   if (mode == 0)
-    k_reduce<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
-                                                     di[2], di[3], di[4], di[5], partials);
+    k_reduce<0><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, words, full, implied3, codes, g, di[0],
+                                                     di[1], di[2], di[3], di[4], di[5],
+                                                     partials);
   else
-    k_reduce<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, full, implied3, codes, g, di[0], di[1],
-                                                     di[2], di[3], di[4], di[5], partials);
+    k_reduce<1><<<kRedBlocks, kRedThreads, 0, st>>>(x, e, words, full, implied3, codes, g, di[0],
+                                                     di[1], di[2], di[3], di[4], di[5],
+                                                     partials);
   k_reduce_final<<<1, 32 * kRedVals, 0, st>>>(partials, out);
   count_launches(2);
   return cudaGetLastError();

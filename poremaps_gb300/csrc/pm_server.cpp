@@ -1,11 +1,13 @@
 // Batched / continuously batching solver (pm_server_* of include/poremaps.h).
 //
 // Requests queue on the host.  A scheduling round (pm_server_step):
-//   1. admits queued requests first come first served while their device
-//      footprint fits the HBM budget and a slot is free (set-up on the
-//      device, then one sweep so every resident sample sits at the start of
-//      an it_eval block: the reference evaluates convergence after the sweeps
-//      it_eval, 2 it_eval, ...);
+//   1. admits queued requests in arrival order while their device footprint
+//      fits the HBM budget and a slot is free; when the head of the queue does
+//      not fit, later requests that do are admitted past it (backfill), at most
+//      max_bypass times before the head goes in, so no request starves.  Each
+//      admission sets the problem up on the device and runs one sweep, so every
+//      resident sample sits at the start of an it_eval block (the reference
+//      evaluates convergence after the sweeps it_eval, 2 it_eval, ...);
 //   2. runs one it_eval block for all resident samples: it_eval batched
 //      launches walking a work table of (sample, fluid-voxel run) items,
 //      captured once per change of the resident set in a CUDA graph, then a
@@ -38,6 +40,7 @@ struct Req {
   pm_params prm;
   std::vector<uint8_t> geom;
   double submit_ms;
+  int bypassed = 0;  // admissions of later requests past this one at the head
 };
 
 struct Res {
@@ -165,31 +168,53 @@ void retire(pm_server* s, Res& r, pm_status st) {
   s->used -= r.bytes;
 }
 
+pm_params request_params(const pm_server* s, const Req& q) {
+  pm_params p = q.prm;
+  p.precision = s->cfg.precision;
+  p.order = PM_ORDER_JACOBI;
+  p.write_log = 0;
+  p.mixed_inner = p.it_eval;  // corrections after iterations 0, it_eval, 2 it_eval, ...
+  p.kernel = 8;               // the batched kernels use the compact correction store
+  return p;
+}
+
+int bypass_limit(const pm_server* s) {
+  return s->cfg.max_bypass == 0 ? 64 : s->cfg.max_bypass;
+}
+
+// How far behind the head the backfill scan looks for a request that fits.
+constexpr size_t kBackfillScan = 256;
+
 pm_status admit(pm_server* s) {
-  while (!s->queue.empty() && (int)s->res.size() < s->cfg.max_resident) {
-    Req& q = s->queue.front();
-    pm_params p = q.prm;
-    p.precision = s->cfg.precision;
-    p.order = PM_ORDER_JACOBI;
-    p.write_log = 0;
-    p.mixed_inner = p.it_eval;  // corrections after iterations 0, it_eval, 2 it_eval, ...
-    p.kernel = 1;               // the batched kernels walk fluid lists
+  size_t i = 0;  // queue position under consideration (0 = head)
+  while (i < s->queue.size() && i < kBackfillScan &&
+         (int)s->res.size() < s->cfg.max_resident) {
+    Req& q = s->queue[i];
+    pm_params p = request_params(s, q);
     size_t bytes = problem_device_bytes(&p);
-    if (s->used + bytes > s->budget) {
-      if (s->res.empty()) {  // can never fit: fail it instead of blocking the queue
-        pm_status e = set_error(PM_ERR_NOMEM, "request needs %zu bytes, budget %zu", bytes,
-                                s->budget);
-        complete(s, q.ticket, e, nullptr, q.submit_ms, now_ms(s));
-        s->queue.pop_front();
-        continue;
-      }
-      break;
+    if (bytes > s->budget) {  // can never fit: fail it instead of blocking the queue
+      pm_status e = set_error(PM_ERR_NOMEM, "request needs %zu bytes, budget %zu", bytes,
+                              s->budget);
+      complete(s, q.ticket, e, nullptr, q.submit_ms, now_ms(s));
+      s->queue.erase(s->queue.begin() + i);
+      continue;
     }
+    // a request behind the head goes in only while the head may still be
+    // passed (backfill on, fewer than max_bypass admissions past it so far)
+    const int lim = bypass_limit(s);
+    if (i > 0 && (lim < 0 || s->queue.front().bypassed >= lim)) break;
+    if (s->used + bytes > s->budget) {
+      if (lim < 0 || s->queue.front().bypassed >= lim) break;  // the head waits
+      ++i;  // does not fit now: look behind it
+      continue;
+    }
+    if (i > 0) s->queue.front().bypassed++;
+    Req qq = std::move(q);
+    s->queue.erase(s->queue.begin() + i);
     pm_problem* pr = nullptr;
-    pm_status st = pm_problem_create(&p, q.geom.data(), &pr);
+    pm_status st = pm_problem_create(&p, qq.geom.data(), &pr);
     if (st != PM_OK) {
-      complete(s, q.ticket, st, nullptr, q.submit_ms, now_ms(s));
-      s->queue.pop_front();
+      complete(s, qq.ticket, st, nullptr, qq.submit_ms, now_ms(s));
       continue;
     }
     // iteration 0 on its own: afterwards every block ends on a check iteration
@@ -198,19 +223,17 @@ pm_status admit(pm_server* s) {
       st = cuda_error(cudaGetLastError(), "admission sweep");
     if (st != PM_OK) {
       pm_problem_destroy(pr);
-      complete(s, q.ticket, st, nullptr, q.submit_ms, now_ms(s));
-      s->queue.pop_front();
+      complete(s, qq.ticket, st, nullptr, qq.submit_ms, now_ms(s));
       continue;
     }
     Res r;
-    r.ticket = q.ticket;
+    r.ticket = qq.ticket;
     r.pr = pr;
-    r.submit_ms = q.submit_ms;
+    r.submit_ms = qq.submit_ms;
     r.admit_ms = now_ms(s);
     r.bytes = bytes;
     r.it = 1;
     s->used += bytes;
-    s->queue.pop_front();
     if (r.it + s->block > p.max_iter) {  // fewer iterations than one block: alone
       retire(s, r, run_tail(r));
       continue;
@@ -341,9 +364,12 @@ pm_status rebuild(pm_server* s) {
     if (mixed(s)) {
       d.X0 = pr->F[pr->cur];
       d.X1 = pr->F[1 - pr->cur];
-      d.E0 = pr->E[0];
-      d.E1 = pr->E[1];
-      d.R = pr->R;
+      d.E0 = pr->Ec[0];
+      d.E1 = pr->Ec[1];
+      d.R = pr->Rc;
+      d.meta = pr->cmeta;
+      d.sa = pr->cslot4;
+      d.sb = pr->cslot2;
       d.ecur0 = 0;
       d.xcur0 = 0;
     } else {
@@ -540,5 +566,38 @@ pm_status pm_server_stats(pm_server* s, double* busy_ms, double* wall_ms, uint64
 }
 
 double pm_server_clock_ms(pm_server* s) { return s ? now_ms(s) : 0.0; }
+
+pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* bytes) {
+  if (!s || !p || !bytes) return set_error(PM_ERR_INVALID, "bad arguments");
+  Req q;
+  q.prm = *p;
+  pm_params rp = request_params(s, q);
+  return pm_problem_footprint(&rp, bytes);
+}
+
+pm_status pm_server_cancel(pm_server* s, uint64_t ticket) {
+  if (!s) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (size_t i = 0; i < s->queue.size(); ++i) {
+    if (s->queue[i].ticket != ticket) continue;
+    complete(s, ticket, PM_ERR_CANCELLED, nullptr, s->queue[i].submit_ms, now_ms(s));
+    s->queue.erase(s->queue.begin() + i);
+    return PM_OK;
+  }
+  for (size_t i = 0; i < s->res.size(); ++i) {
+    if (s->res[i].ticket != ticket) continue;
+    // between rounds the server stream is idle: free the sample now and
+    // rebuild the work table (and graph) for the rest before the next round
+    Res r = s->res[i];
+    s->res.erase(s->res.begin() + i);
+    complete(s, ticket, PM_ERR_CANCELLED, nullptr, r.submit_ms, r.admit_ms);
+    pm_problem_destroy(r.pr);
+    s->used -= r.bytes;
+    s->dirty = true;
+    return PM_OK;
+  }
+  return set_error(PM_ERR_NOT_FOUND, "ticket %llu is not queued or resident",
+                   (unsigned long long)ticket);
+}
 
 }  // extern "C"

@@ -150,3 +150,51 @@ def test_tensor_axis_mapping():
     off = np.abs(K - np.diag(np.diag(K))).max()
     # no path along y or z: those responses vanish up to the stopping error
     assert abs(K[1, 1]) <= 1e-6 * kz and abs(K[2, 2]) <= 1e-6 * kz and off <= 1e-6 * kz
+
+
+def test_cli_report_full_precision(tmp_path):
+    """poremaps_gpu --report out.json: the report's iteration count is the
+    log's last row and its wk33, printed at full precision, rounds to the
+    log's 7 digits and equals, bit for bit, the oracle's run of the same
+    case in the reference order."""
+    name = "spheres_converged"
+    run_cli(name, tmp_path, ["--order", "reference", "--arith", "exact",
+                             "--report", "rep.json"])
+    rep = json.loads((tmp_path / "rep.json").read_text())
+    last = [c.strip() for c in str(GOLDEN[f"{name}/log"]).strip().splitlines()[-1].split(",")]
+    r = rep["result"]
+    assert rep["status"] == "ok" and r["converged"] == 1
+    assert r["iterations"] == int(last[0])
+    assert f"{r['wk33']:e}" == last[-1]
+    c = META[name]
+    orc = OracleProblem(make_golden.geometry(c["geom"]), c["bc"], c["solver"], c.get("dx", 1e-5))
+    ro = orc.calc_flow(c["max_iter"], 100, 100, c["eps"], "reference")
+    assert r["wk33"] == ro.wk33 and r["wk13"] == ro.wk13 and r["wk23"] == ro.wk23
+
+
+def test_cli_tensor(tmp_path):
+    """poremaps_gpu --tensor: the three axis-rotated solves of the .inp's
+    geometry give the reference program's tensor (16^3 sphere pack, SOR) to
+    1e-6 of its scale, and the report carries all nine components."""
+    c = META["tensor_s3_z"]
+    g = make_golden.geometry(dict(make_golden.TENSOR_GEOM))
+    nz, ny, nx = g.shape
+    g.tofile(tmp_path / "geom.raw")
+    (tmp_path / "in.inp").write_text(make_golden.inp_text(dict(c, max_iter=400000), nx, ny, nz))
+    r = subprocess.run([pm.CLI_PATH, "in.inp", "--tensor", "--report", "rep.json"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rep = json.loads((tmp_path / "rep.json").read_text())
+    K = np.array(rep["tensor_m2"]).reshape(3, 3)
+    K_ref = np.zeros((3, 3))
+    slots = {"x": ((1, 0), (2, 0), (0, 0)), "y": ((2, 1), (0, 1), (1, 1)),
+             "z": ((0, 2), (1, 2), (2, 2))}
+    for rot in "xyz":
+        last = [v.strip() for v in
+                str(GOLDEN[f"tensor_s3_{rot}/log"]).strip().splitlines()[-1].split(",")]
+        for (i, j), lv in zip(slots[rot], last[-3:]):
+            K_ref[i, j] = float(lv)
+    scale = np.abs(np.diag(K_ref)).max()
+    assert np.abs(K - K_ref).max() <= 2e-6 * scale
+    assert len(rep["solves"]) == 3 and all(s["converged"] == 1 for s in rep["solves"])
+    assert not (tmp_path / "run.log").exists()

@@ -97,21 +97,15 @@ def test_graphs_and_autotune_do_not_change_results():
             assert other[i].result.wk33 == base[i].result.wk33
 
 
-def footprint(shape):
-    """Device bytes of one mixed-precision request (mirrors the library's layout)."""
-    nz, ny, nx = shape
-    NX, NY, NZ = nx + 4, ny + 4, nz + 4
-    up = lambda a, b: (a + b - 1) // b * b  # noqa: E731
-    a64 = up(14 + NX, 16) * NY * NZ + 64
-    a4 = up(6 + NX, 8) * NY * NZ + 16
-    ac = up(14 + NX, 16) * NY * NZ + 256
-    n = nx * ny * nz
-    return ac + 4 * n + 64 * a64 + 48 * a4 + 8 * n + (1 << 20)
+def footprint(g):
+    """Device bytes the server admits one request of this geometry by."""
+    with pm.Server(precision="mixed") as s:
+        return s.request_bytes(g, **KW)
 
 
 def test_budget_limits_resident_set_and_all_finish():
     geoms = samples(6, seed=4)
-    budget = int(2.5 * max(footprint(g.shape) for g in geoms))
+    budget = int(2.5 * max(footprint(g) for g in geoms))
     res = run_server(geoms, budget=budget)
     assert len(res) == len(geoms) and all(c.status == 0 for c in res.values())
     # some request had to wait for an earlier one to retire
@@ -226,3 +220,111 @@ def test_server_eps_fixed_point_matches_single_problem():
         assert c.status == 0 and c.result.converged and r.converged
         assert c.result.iterations < 100000 and abs(c.result.iterations - r.iterations) <= 5000
         assert abs(c.result.wk33 - r.wk33) <= 1e-12 * abs(r.wk33)
+
+
+def drain(s, tickets, limit=5000):
+    out, steps = {}, 0
+    while len(out) < len(tickets):
+        s.step()
+        steps += 1
+        for c in s.poll():
+            out[tickets[c.ticket]] = c
+        assert steps < limit
+    return out
+
+
+def test_request_larger_than_budget_fails_with_nomem():
+    """A request whose footprint exceeds the whole budget completes at once
+    with PM_ERR_NOMEM while a resident request keeps running; a small one
+    behind it still completes."""
+    big = synth.sphere_pack((64, 64, 64), rmin=2.0, rmax=4.0, solid_fraction=0.55, seed=3)
+    small = samples(2, seed=4)
+    budget = footprint(small[0]) + footprint(small[1]) + 4096
+    assert footprint(big) > budget
+    s = pm.Server(precision="mixed", hbm_budget_bytes=budget)
+    tickets = {s.submit(small[0], **KW): "a"}
+    s.step()  # "a" resident
+    tickets[s.submit(big, **KW)] = "big"
+    tickets[s.submit(small[1], **KW)] = "b"
+    res = drain(s, tickets)
+    s.close()
+    assert res["big"].status == pm.PM_ERR_NOMEM
+    assert res["a"].status == 0 and res["b"].status == 0
+    r = single(small[1])
+    assert res["b"].result.wk33 == r.wk33 and res["b"].result.iterations == r.iterations
+
+
+def _backfill_case(max_bypass):
+    a = synth.sphere_pack((32, 32, 32), rmin=1.5, rmax=3.0, solid_fraction=0.55, seed=21)
+    b = synth.sphere_pack((28, 28, 30), rmin=1.5, rmax=3.0, solid_fraction=0.55, seed=22)
+    c1 = synth.sphere_pack((12, 12, 12), rmin=1.5, rmax=3.0, solid_fraction=0.55, seed=23)
+    c2 = synth.sphere_pack((12, 14, 12), rmin=1.5, rmax=3.0, solid_fraction=0.55, seed=24)
+    budget = footprint(a) + footprint(c1) + footprint(c2) + 4096
+    assert footprint(b) < footprint(a) and footprint(a) + footprint(b) > budget
+    s = pm.Server(precision="mixed", hbm_budget_bytes=budget, max_bypass=max_bypass)
+    tickets = {}
+    for name, g in (("a", a), ("b", b), ("c1", c1), ("c2", c2)):
+        tickets[s.submit(g, **KW)] = name
+    res = drain(s, tickets)
+    s.close()
+    assert all(c.status == 0 for c in res.values())
+    for name, g in (("b", b), ("c1", c1)):
+        assert res[name].result.wk33 == single(g).wk33
+    return {k: c.admit_ms for k, c in res.items()}
+
+
+def test_backfill_admits_past_a_head_that_does_not_fit():
+    """a is resident, b does not fit beside it: c1 and c2 behind b fit and are
+    admitted before b (default backfill)."""
+    t = _backfill_case(0)
+    assert t["c1"] < t["b"] and t["c2"] < t["b"]
+
+
+def test_backfill_bypass_limit_and_strict_fifo():
+    """With max_bypass 1 only c1 passes b; with backfill off (-1) neither does."""
+    t = _backfill_case(1)
+    assert t["c1"] < t["b"] <= t["c2"]
+    t = _backfill_case(-1)
+    assert t["b"] <= t["c1"] and t["b"] <= t["c2"]
+
+
+def test_cancel_queued_and_resident():
+    """Cancelling a resident and a queued request frees them; the others
+    finish with the results they have alone."""
+    geoms = samples(4, seed=6)
+    s = pm.Server(precision="mixed", max_resident=2)
+    tickets = {s.submit(g, **KW): i for i, g in enumerate(geoms)}
+    inv = {i: t for t, i in tickets.items()}
+    s.step()  # 0 and 1 resident, 2 and 3 queued
+    assert s.cancel(inv[0]) == 0
+    assert s.cancel(inv[3]) == 0
+    assert s.cancel(10**9) == pm.PM_ERR_NOT_FOUND
+    res = drain(s, tickets)
+    assert s.cancel(inv[1]) == pm.PM_ERR_NOT_FOUND  # already completed
+    s.close()
+    assert res[0].status == pm.PM_ERR_CANCELLED and res[3].status == pm.PM_ERR_CANCELLED
+    for i in (1, 2):
+        r = single(geoms[i])
+        assert res[i].status == 0 and res[i].result.wk33 == r.wk33
+        assert res[i].result.iterations == r.iterations
+
+
+def test_allocation_failure_is_reported_and_recovered():
+    """A failed device allocation during set-up (injected on the host) gives
+    PM_ERR_NOMEM from pm_problem_create and in the server's completion;
+    nothing leaks and the next requests run normally."""
+    g = samples(2, seed=8)
+    for nth in (1, 3, 6):
+        pm.debug_fail_alloc(nth)
+        with pytest.raises(RuntimeError, match="PM_ERR_NOMEM"):
+            pm.Problem(g[0], None, precision="mixed", order="jacobi", **KW)
+    pm.debug_fail_alloc(0)
+    ref = single(g[1])
+    s = pm.Server(precision="mixed")
+    pm.debug_fail_alloc(2)
+    tickets = {s.submit(x, **KW): i for i, x in enumerate(g)}
+    res = drain(s, tickets)
+    pm.debug_fail_alloc(0)
+    s.close()
+    assert res[0].status == pm.PM_ERR_NOMEM
+    assert res[1].status == 0 and res[1].result.wk33 == ref.wk33

@@ -82,3 +82,41 @@ def test_noalloc_rejects_sizes_beyond_the_scratch():
     dummy = C.c_void_p(16)
     st = lib.pm_reduce_fields_noalloc(size, dummy, dummy, dummy, dummy, dummy, None, dummy, None)
     assert st == 1 and b"scratch" in lib.pm_last_error()
+
+
+def test_noalloc_without_box_on_a_caller_stream():
+    """dom_interest NULL: the box sums are 0 and the whole-domain sums still
+    match pm_compute_permeability; the launch goes on a stream the caller
+    owns, which the caller synchronises before reading the sums."""
+    geom = synth.random_solid((18, 14, 22), 0.3, 29)
+    nz, ny, nx = geom.shape
+    dx = 2e-5
+    with pm.Problem(geom, None, boundary_method=1, solving_algorithm=3, voxel_size=dx,
+                    order="redblack") as pr:
+        pr.iterate(250)
+        ref = pr.permeability()
+        u, v, w, p = pr.fields()
+        phi = pr.porosity()
+    dev = torch.device("cuda", 0)
+    g_d = torch.from_numpy(geom.copy()).to(dev)
+    f_d = [torch.from_numpy(a.copy()).to(dev) for a in (u, v, w, p)]
+    sums = torch.empty(9, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream()
+    size = (C.c_int * 3)(nx, ny, nz)
+    lib = pm.load_library()
+    for call in range(2):
+        sums.fill_(float("nan"))
+        torch.cuda.synchronize()
+        st = lib.pm_reduce_fields_noalloc(size, g_d.data_ptr(), *[t.data_ptr() for t in f_d],
+                                          None, sums.data_ptr(), C.c_void_p(stream.cuda_stream))
+        assert st == 0, lib.pm_last_error()
+        stream.synchronize()
+        s = sums.cpu().numpy()
+        assert np.all(s[4:9] == 0.0), (call, s[4:9])
+        wfl = int((geom == 0).sum())
+        for name, val in (("wk13", s[0] / wfl / RE * phi * dx * dx),
+                          ("wk23", s[1] / wfl / RE * phi * dx * dx),
+                          ("wk33", s[2] / wfl / RE * phi * dx * dx),
+                          ("wmax_velz", s[3] * dx)):
+            want = getattr(ref, name)
+            assert abs(val - want) <= 1e-12 * max(abs(want), 1e-300), (call, name, val, want)
