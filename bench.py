@@ -433,7 +433,8 @@ def kernel_traffic(kid, brick, size, nvox):
 # Sources of each correction-sweep kernel: a traffic capture is valid while
 # their SHA-256 is the one recorded with it.
 KERNEL_SOURCES = ["poremaps_gb300/csrc/pm_fast.cu", "poremaps_gb300/csrc/pm_compact.cu",
-                  "poremaps_gb300/csrc/pm_stencil.cuh", "poremaps_gb300/csrc/pm_internal.h"]
+                  "poremaps_gb300/csrc/pm_compact.cuh", "poremaps_gb300/csrc/pm_stencil.cuh",
+                  "poremaps_gb300/csrc/pm_internal.h"]
 
 
 def write_traffic(csv_path, kid, brick, size):

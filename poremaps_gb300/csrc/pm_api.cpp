@@ -637,7 +637,7 @@ size_t problem_device_bytes(const pm_params* p) {
   const bool cpt = p->kernel == 8 || p->kernel == 9;
   if (p->precision == PM_PREC_MIXED && !cpt) b += 3 * sizeof(float4) * (size_t)g.alloc4;
   if (p->precision == PM_PREC_MIXED && (cpt || p->kernel < 0))
-    b += (3 * sizeof(float4) + sizeof(int4) + sizeof(int2) + sizeof(uint16_t)) *
+    b += (3 * sizeof(float4) + sizeof(int4) + sizeof(int2) + sizeof(unsigned)) *
              ((size_t)g.nvox + 1) +
          sizeof(uint2) * (size_t)compact_words(g);
   b += 8 * (size_t)g.nvox;  // export scratch
@@ -790,7 +790,7 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       pr->Rc = pr->c_base + 2 * nl;
       CKF(dev_alloc((void**)&pr->cslot4, sizeof(int4) * nl));
       CKF(dev_alloc((void**)&pr->cslot2, sizeof(int2) * nl));
-      CKF(dev_alloc((void**)&pr->cmeta, sizeof(uint16_t) * nl));
+      CKF(dev_alloc((void**)&pr->cmeta, sizeof(unsigned) * nl));
       CKF(dev_alloc((void**)&pr->cwords, sizeof(uint2) * (size_t)compact_words(g)));
     }
     pm_status ts = choose_correction_kernel(pr, p->kernel);

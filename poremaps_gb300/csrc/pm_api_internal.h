@@ -92,7 +92,7 @@ struct pm_problem {
   float4* Rc = nullptr;
   int4* cslot4 = nullptr;
   int2* cslot2 = nullptr;
-  uint16_t* cmeta = nullptr;
+  unsigned* cmeta = nullptr;
   uint2* cwords = nullptr;
   double* partials = nullptr;
   double* dout = nullptr;

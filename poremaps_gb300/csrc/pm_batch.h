@@ -12,7 +12,7 @@ struct SampleDesc {
   float4 *E0, *E1, *R;    // FP32 correction (ping-pong) and residual: the compact store,
                           // one float4 (u, v, w, p) per fluid-list position and a zero slot
   const uint8_t* codes;
-  const uint16_t* meta;   // compact store: code and plane flags per list position
+  const unsigned* meta;   // compact store: code and plane flags per list position
   const int4* sa;         // compact store: x L, x R, y L, y R neighbour positions
   const int2* sb;         // compact store: z L, z R neighbour positions
   const int* list;

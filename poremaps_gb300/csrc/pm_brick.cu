@@ -14,6 +14,7 @@
 // operands as the global-memory kernels, so the fields are bitwise identical.
 // The wait is bounded: on expiry the CTA records an error, waits (bounded) for
 // its copy still in flight and returns.
+#include <atomic>
 #include <vector>
 
 #include "pm_brick.h"
@@ -129,8 +130,8 @@ __global__ void k_brick_starts(const int* list, int n, Grid g, int bx, int by, i
 
 template <class S>
 void set_smem_attr() {
-  static bool done = false;
-  if (done) return;
+  static std::atomic<bool> done{false};
+  if (done.load()) return;
   cudaFuncSetAttribute(k_brick_inner<S, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)S::SMEM);
   cudaFuncSetAttribute(k_brick_inner<S, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

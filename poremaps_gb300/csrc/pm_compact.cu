@@ -40,7 +40,7 @@ template <int SOLVER, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_dc_inner_c(const float4* __restrict__ E,
                                                          float4* __restrict__ E2,
                                                          const float4* __restrict__ R,
-                                                         const uint16_t* __restrict__ meta,
+                                                         const unsigned* __restrict__ meta,
                                                          const int4* __restrict__ sa,
                                                          const int2* __restrict__ sb,
                                                          int nlist) {
@@ -135,7 +135,7 @@ __device__ __forceinline__ int list_pos(const uint2* words, int nw, const Grid& 
 
 // Slots and metadata of every list position (see CompactSlots).
 __global__ void k_compact_slots(const uint8_t* codes, Grid g, int nw, const int* list, int nlist,
-                                const uint2* words, int4* sa, int2* sb, uint16_t* meta) {
+                                const uint2* words, int4* sa, int2* sb, unsigned* meta) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
     int x, y, z;
     interior_xyz(list[q], g, x, y, z);
@@ -159,7 +159,7 @@ __global__ void k_compact_slots(const uint8_t* codes, Grid g, int nw, const int*
     }
     sa[q] = make_int4(slot[0], slot[1], slot[2], slot[3]);
     sb[q] = make_int2(slot[4], slot[5]);
-    meta[q] = (uint16_t)(code | (z == 0 ? kMetaZFirst : 0u) | (z == g.nz - 1 ? kMetaZLast : 0u));
+    meta[q] = make_meta(cs[0], cs[1], cs[2], z == 0, z == g.nz - 1);
   }
 }
 
@@ -177,7 +177,7 @@ long long compact_words(const Grid& g) {
 }
 
 cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, int nlist,
-                          uint2* words, int4* sa, int2* sb, uint16_t* meta, cudaStream_t st) {
+                          uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st) {
   const int nw = (g.nx + 31) / 32;
   const long long nwords = compact_words(g) - 1;
   const int sms = sm_count();
@@ -191,7 +191,7 @@ cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, 
 
 template <int MINB>
 static cudaError_t inner_c_launch(const float4* e, float4* e2, const float4* r,
-                                  const uint16_t* meta, const int4* sa, const int2* sb,
+                                  const unsigned* meta, const int4* sa, const int2* sb,
                                   int nlist, int solver, cudaStream_t st) {
   if (nlist < 1) return cudaSuccess;
   const int blocks = grid_for(nlist, 256, MINB * sm_count());
@@ -202,7 +202,7 @@ static cudaError_t inner_c_launch(const float4* e, float4* e2, const float4* r,
   return cudaGetLastError();
 }
 
-cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, const uint16_t* meta,
+cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, const unsigned* meta,
                               const int4* sa, const int2* sb, int nlist, int solver, int minb,
                               cudaStream_t st) {
   if (minb <= 2) return inner_c_launch<2>(e, e2, r, meta, sa, sb, nlist, solver, st);

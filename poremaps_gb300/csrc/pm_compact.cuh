@@ -50,9 +50,25 @@ struct CompactSlots {
   int2 b;  // z L, z R
 };
 
-// Per-voxel metadata: the code byte 1..216 and two plane flags.
-constexpr unsigned kMetaZFirst = 1u << 8;  // first interior plane: -z pressure reads 0
-constexpr unsigned kMetaZLast = 1u << 9;   // last interior plane: own pressure reads 0
+// Per-voxel metadata (32 bits): the three neighbourhood cases (3 bits each,
+// x in bits 0-2), two plane flags and which +-1 neighbours are fluid.
+constexpr unsigned kMetaZFirst = 1u << 9;   // first interior plane: -z pressure reads 0
+constexpr unsigned kMetaZLast = 1u << 10;   // last interior plane: own pressure reads 0
+constexpr int kMetaFluidShift = 11;         // bits 11 + 2 axis (+1): -side (+side) fluid
+
+__device__ __forceinline__ unsigned make_meta(int cx, int cy, int cz, bool zfirst, bool zlast);
+
+__device__ __forceinline__ unsigned make_meta(int cx, int cy, int cz, bool zfirst, bool zlast) {
+  unsigned m = (unsigned)cx | ((unsigned)cy << 3) | ((unsigned)cz << 6);
+  if (zfirst) m |= kMetaZFirst;
+  if (zlast) m |= kMetaZLast;
+  const int c[3] = {cx, cy, cz};
+  for (int a = 0; a < 3; ++a) {
+    if (left_fluid(c[a])) m |= 1u << (kMetaFluidShift + 2 * a);
+    if (right_fluid(c[a])) m |= 1u << (kMetaFluidShift + 2 * a + 1);
+  }
+  return m;
+}
 
 __device__ __forceinline__ int word_rank(uint2 w, int x) {
   return (int)w.y + __popc(w.x & ((1u << (x & 31)) - 1u));
@@ -71,9 +87,8 @@ __device__ __forceinline__ void inner_c_compute(const float4* __restrict__ E,
                                                 float4* __restrict__ E2,
                                                 const float4* __restrict__ R, int i,
                                                 unsigned meta, const CompactSlots& sl) {
-  const int code = (int)(meta & 0xffu);
-  int cx, cy, cz;
-  decode_cases(code, cx, cy, cz);
+  const int cx = (int)(meta & 7u), cy = (int)((meta >> 3) & 7u), cz = (int)((meta >> 6) & 7u);
+  auto fl = [&](int axis, int side) { return (meta >> (kMetaFluidShift + 2 * axis + side)) & 1u; };
   const float4 C = __ldg(E + i);
   const float4 XL = __ldg(E + sl.a.x), XR = __ldg(E + sl.a.y);
   const float4 YL = __ldg(E + sl.a.z), YR = __ldg(E + sl.a.w);
@@ -85,18 +100,18 @@ __device__ __forceinline__ void inner_c_compute(const float4* __restrict__ E,
   // the wall stencils across an axis take (ll, l, r, rr) = (R, L, R, L),
   // which case_pick resolves to exactly the points each case uses
   s.uc = C.x;
-  s.uxm = left_fluid(cx) ? XL.x : 0.f;
-  s.uxp = right_fluid(cx) ? XR.x : 0.f;
+  s.uxm = fl(0, 0) ? XL.x : 0.f;
+  s.uxp = fl(0, 1) ? XR.x : 0.f;
   s.uymm = YR.x; s.uym = YL.x; s.uyp = YR.x; s.uypp = YL.x;
   s.uzmm = ZR.x; s.uzm = ZL.x; s.uzp = ZR.x; s.uzpp = ZL.x;
   s.vc = C.y;
-  s.vym = left_fluid(cy) ? YL.y : 0.f;
-  s.vyp = right_fluid(cy) ? YR.y : 0.f;
+  s.vym = fl(1, 0) ? YL.y : 0.f;
+  s.vyp = fl(1, 1) ? YR.y : 0.f;
   s.vxmm = XR.y; s.vxm = XL.y; s.vxp = XR.y; s.vxpp = XL.y;
   s.vzmm = ZR.y; s.vzm = ZL.y; s.vzp = ZR.y; s.vzpp = ZL.y;
   s.wc = C.z;
-  s.wzm = left_fluid(cz) ? ZL.z : 0.f;
-  s.wzp = right_fluid(cz) ? ZR.z : 0.f;
+  s.wzm = fl(2, 0) ? ZL.z : 0.f;
+  s.wzp = fl(2, 1) ? ZR.z : 0.f;
   s.wxmm = XR.z; s.wxm = XL.z; s.wxp = XR.z; s.wxpp = XL.z;
   s.wymm = YR.z; s.wym = YL.z; s.wyp = YR.z; s.wypp = YL.z;
   // a pressure difference is taken only where the -side neighbour is fluid,
@@ -107,7 +122,7 @@ __device__ __forceinline__ void inner_c_compute(const float4* __restrict__ E,
   s.pym = YL.w;
   s.pzm = (meta & kMetaZFirst) ? 0.f : ZL.w;
   float un, vn, wn, pn;
-  update_fast<float, SOLVER>(s, code, un, vn, wn, pn);
+  update_fast_cases<float, SOLVER>(s, cx, cy, cz, un, vn, wn, pn);
   E2[i] = make_float4(un + r.x, vn + r.y, wn + r.z, pn + r.w);
 }
 
@@ -116,7 +131,7 @@ template <int SOLVER>
 __device__ __forceinline__ void inner_c_voxel(const float4* __restrict__ E,
                                               float4* __restrict__ E2,
                                               const float4* __restrict__ R,
-                                              const uint16_t* __restrict__ meta,
+                                              const unsigned* __restrict__ meta,
                                               const int4* __restrict__ sa,
                                               const int2* __restrict__ sb, int i) {
   CompactSlots sl;

@@ -178,10 +178,9 @@ __device__ __forceinline__ T vel_fast(T c, T am, T ap, int cs1, T ll1, T l1, T r
 }
 
 template <typename T, int SOLVER>
-__device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un, T& vn, T& wn,
-                                            T& pn, const T* ctab = nullptr) {
-  int cx, cy, cz;
-  decode_cases(code, cx, cy, cz);
+__device__ __forceinline__ void update_fast_cases(const Stencil<T>& s, int cx, int cy, int cz,
+                                                  T& un, T& vn, T& wn, T& pn,
+                                                  const T* ctab = nullptr) {
   const bool lx = left_solid(cx), ly = left_solid(cy), lz = left_solid(cz);
   const T dpx = lx ? T(0) : s.pc - s.pxm;
   const T dpy = ly ? T(0) : s.pc - s.pym;
@@ -199,6 +198,14 @@ __device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un
                            s.wym, s.wyp, s.wypp, dpz, lz, ctab);
   T div = (SOLVER == 1) ? div0 : ((s.wzp - wn) + (s.vyp - vn)) + (s.uxp - un);
   pn = fma(T(-kC2 * kDt), div, s.pc);
+}
+
+template <typename T, int SOLVER>
+__device__ __forceinline__ void update_fast(const Stencil<T>& s, int code, T& un, T& vn, T& wn,
+                                            T& pn, const T* ctab = nullptr) {
+  int cx, cy, cz;
+  decode_cases(code, cx, cy, cz);
+  update_fast_cases<T, SOLVER>(s, cx, cy, cz, un, vn, wn, pn, ctab);
 }
 
 // Gather of the stencil values of one interior voxel.

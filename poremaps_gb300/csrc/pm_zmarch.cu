@@ -15,8 +15,11 @@
 // Every mbarrier wait is bounded (clock64 budget); on expiry the CTA records
 // an error code, drains its own copies still in flight (again bounded) and
 // returns, so a broken pipeline never hangs the device.
+#include <atomic>
+
 #include "pm_stencil.cuh"
 #include "pm_tma.cuh"
+
 #include "pm_zmarch.h"
 
 namespace pm {
@@ -210,15 +213,17 @@ __global__ void __launch_bounds__(T::THREADS)
 namespace tma {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once; the initialisation of a function-local static is
+  // thread-safe (problems are created from several host threads at once)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -250,8 +255,8 @@ int zmarch_available() { return tma::encode_fn() != nullptr; }
 
 template <class T>
 static void set_smem_attr() {
-  static bool done = false;
-  if (done) return;
+  static std::atomic<bool> done{false};
+  if (done.load()) return;
   cudaFuncSetAttribute(k_zmarch_inner<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(Smem<T>));
   cudaFuncSetAttribute(k_zmarch_inner<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
