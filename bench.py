@@ -50,6 +50,9 @@ def parse():
                     help="skip the batched-stream (c4) and request-stream (c5) legs that the "
                          "default single-GPU run adds to its line")
     ap.add_argument("--c4-samples", type=int, default=256)
+    ap.add_argument("--relaunch-sweeps", type=int, default=0,
+                    help="c4/c5: 1 = the server launches every FP32 sweep separately instead "
+                         "of one persistent kernel per round")
     ap.add_argument("--c5-requests", type=int, default=48)
     ap.add_argument("--c5-max-axis", type=int, default=192)
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
@@ -608,7 +611,7 @@ def unconverged(results):
     return [i for i, r in enumerate(results) if not r.converged]
 
 
-def c4_result(n_samples: int):
+def c4_result(n_samples: int, relaunch: int = 0):
     """The batched uneven stream (configuration 4) through the mixed-precision
     server against the plain FP64 form solving the samples one by one."""
     import poremaps_gb300 as pm
@@ -618,7 +621,7 @@ def c4_result(n_samples: int):
     t_gen = time.perf_counter() - t_gen
     nvox = sum(g.size for g, _ in reqs)
     # batched mixed-precision server
-    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1)
+    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1, relaunch_sweeps=relaunch)
     t0 = time.perf_counter()
     tickets = {srv.submit(g, boundary_method=bc, **SERVE_KW): i for i, (g, bc) in enumerate(reqs)}
     done = {}
@@ -677,7 +680,7 @@ def run_c4(args):
     import poremaps_gb300 as pm
 
     pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps(c4_result(args.samples)), flush=True)
+    print(json.dumps(c4_result(args.samples, args.relaunch_sweeps)), flush=True)
     return 0
 
 
@@ -688,7 +691,7 @@ def pcts(lat, skip=()):
     return {"p50_s": float(np.percentile(keep, 50)), "p99_s": float(np.percentile(keep, 99))}
 
 
-def c5_result(n_requests: int, max_axis: int):
+def c5_result(n_requests: int, max_axis: int, relaunch: int = 0):
     """A serving stream (configuration 5): Poisson arrivals through the
     mixed-precision server, and the plain FP64 form serving the same arrivals
     one request at a time."""
@@ -698,7 +701,7 @@ def c5_result(n_requests: int, max_axis: int):
     # arrival rate: keep the device busy -- mean inter-arrival = 0.6 x the mean
     # solve time estimated from the first request alone (scaled by voxels)
     rng = np.random.default_rng(55)
-    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1)
+    srv = pm.Server(precision="mixed", use_graphs=1, autotune=1, relaunch_sweeps=relaunch)
     probe = time.perf_counter()
     t = {srv.submit(reqs[0][0], boundary_method=reqs[0][1], **SERVE_KW): 0}
     while srv.step():
@@ -783,7 +786,7 @@ def run_c5(args):
     import poremaps_gb300 as pm
 
     pm.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps(c5_result(args.samples, args.max_axis)), flush=True)
+    print(json.dumps(c5_result(args.samples, args.max_axis, args.relaunch_sweeps)), flush=True)
     return 0
 
 

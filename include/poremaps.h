@@ -275,6 +275,9 @@ typedef struct {
                                head is admitted (0 = 64; negative = strict first come,
                                first served).  A request larger than the whole budget
                                completes at once with PM_ERR_NOMEM. */
+  int relaunch_sweeps;      /* mixed form: 0 (default) runs a round's FP32 sweeps as one
+                               persistent kernel walking a device tile queue; 1 launches
+                               every sweep separately (same results bit for bit) */
 } pm_server_config;
 
 typedef struct pm_server pm_server;
@@ -315,6 +318,19 @@ pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* byte
  * their PM_ERR_NOMEM handling on the host without exhausting a GPU; 0 clears
  * it.  Process-wide. */
 pm_status pm_debug_fail_alloc(int nth);
+/* Makes the waits of the server's persistent sweep kernel (mixed form) wait
+ * for `extra` more finished items than exist, with at most `polls` polls
+ * (0 = the kernel's own limit of a few seconds), so a test can see a wait run
+ * out: the kernel sets its error flag and returns, pm_server_step reports
+ * PM_ERR_CUDA, and the device stays usable.  Takes effect for rounds captured
+ * after the call; 0, 0 restores normal operation.  Process-wide. */
+pm_status pm_debug_round_wait(unsigned extra, int polls);
+/* While on, every launch of the TMA z-march correction sweep (kernels 0 and 3)
+ * reports its first pipeline wait as timed out without waiting: each CTA sets
+ * the error flag, waits (bounded) for its copies in flight and returns, and
+ * the sweep's caller gets PM_ERR_CUDA with the device still usable.  0 turns
+ * it off.  Process-wide. */
+pm_status pm_debug_tma_fail(int on);
 
 #ifdef __cplusplus
 }

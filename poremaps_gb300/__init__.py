@@ -71,7 +71,7 @@ class Result(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int),
                 ("precision", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
-                ("max_bypass", C.c_int)]
+                ("max_bypass", C.c_int), ("relaunch_sweeps", C.c_int)]
 
 
 class Completion(C.Structure):
@@ -90,7 +90,8 @@ EXPORTS = ["pm_last_error", "pm_last_error_copy", "pm_version", "pm_params_defau
            "pm_server_create", "pm_server_destroy",
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms", "pm_server_cancel", "pm_debug_fail_alloc",
-           "pm_problem_footprint", "pm_server_request_bytes"]
+           "pm_problem_footprint", "pm_server_request_bytes", "pm_debug_round_wait",
+           "pm_debug_tma_fail"]
 
 _lib = None
 
@@ -149,6 +150,8 @@ def load_library(path: str = LIB_PATH):
         "pm_server_clock_ms": (C.c_double, [vp]),
         "pm_server_cancel": (C.c_int, [vp, C.c_uint64]),
         "pm_debug_fail_alloc": (C.c_int, [C.c_int]),
+        "pm_debug_round_wait": (C.c_int, [C.c_uint, C.c_int]),
+        "pm_debug_tma_fail": (C.c_int, [C.c_int]),
         "pm_problem_footprint": (C.c_int, [P(Params), P(C.c_size_t)]),
         "pm_server_request_bytes": (C.c_int, [vp, P(Params), P(C.c_size_t)]),
     }
@@ -176,6 +179,17 @@ def debug_fail_alloc(nth: int) -> None:
     """pm_debug_fail_alloc: the nth device allocation of problem set-up from
     now on fails as out of memory (0 clears)."""
     _check(load_library().pm_debug_fail_alloc(int(nth)))
+
+
+def debug_round_wait(extra: int, polls: int) -> None:
+    """pm_debug_round_wait: the server's persistent sweep waits for `extra`
+    items that never finish, with at most `polls` polls (0, 0 restores)."""
+    _check(load_library().pm_debug_round_wait(int(extra), int(polls)))
+
+
+def debug_tma_fail(on: bool) -> None:
+    """pm_debug_tma_fail: z-march launches report a timed-out first wait."""
+    _check(load_library().pm_debug_tma_fail(int(bool(on))))
 
 
 def _check(st: int):
@@ -382,10 +396,10 @@ class Server:
 
     def __init__(self, precision: str | int = "mixed", hbm_budget_bytes: int = 0,
                  max_resident: int = 0, use_graphs: int = 1, autotune: int = 0,
-                 max_bypass: int = 0):
+                 max_bypass: int = 0, relaunch_sweeps: int = 0):
         cfg = ServerConfig(hbm_budget_bytes, max_resident,
                            PRECISIONS.get(precision, precision), use_graphs, autotune,
-                           max_bypass)
+                           max_bypass, relaunch_sweeps)
         self.h = C.c_void_p()
         _check(load_library().pm_server_create(C.byref(cfg), C.byref(self.h)))
 

@@ -669,6 +669,11 @@ pm_status pm_problem_footprint(const pm_params* p, size_t* bytes) {
   return PM_OK;
 }
 
+pm_status pm_debug_tma_fail(int on) {
+  zmarch_debug_fail(on);
+  return PM_OK;
+}
+
 pm_status pm_debug_fail_alloc(int nth) {
   if (nth < 0) return set_error(PM_ERR_INVALID, "nth must be >= 0");
   g_fail_alloc.store(nth);

@@ -125,6 +125,78 @@ __global__ void k_batch_sumw(const SampleDesc* d, const WorkItem* items, int nit
   }
 }
 
+// Acquire-load polls of a counter until it reaches target, bounded: about
+// 2^24 polls of >= 128 ns each (seconds, against a sweep of one round that
+// takes microseconds to a millisecond).
+constexpr int kMaxPolls = 1 << 24;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool wait_at_least(const unsigned* p, unsigned target, int polls) {
+  for (int i = 0; i < polls; ++i) {
+    if (ld_acquire(p) >= target) return true;
+    __nanosleep(128);
+  }
+  return false;
+}
+
+// Persistent round of FP32 correction sweeps (see launch_batch_round).
+// Progress: a ticket waits only on tickets of the previous sweep, which were
+// handed out before it to CTAs that are running, so the smallest unfinished
+// ticket never waits and no CTA needs another to be co-resident.  A sample's
+// items are at most one sweep apart, so sweep k (reading buffer k - 1,
+// writing the buffer sweep k - 2 wrote) never overwrites a value that a
+// sweep-(k - 1) item still reads.  Corrections and residuals are read with
+// L1-bypassing loads: other CTAs wrote them in this launch.
+template <int S>
+__global__ void __launch_bounds__(256, 4)
+    k_batch_inner_round(const SampleDesc* d, const WorkItem* items, int nitems, int sweeps,
+                        unsigned* sync, unsigned extra, int polls) {
+  __shared__ __align__(16) SampleDesc sd;
+  __shared__ unsigned sh_t;
+  __shared__ int sh_ok;
+  const unsigned total = (unsigned)sweeps * (unsigned)nitems;
+  for (;;) {
+    __syncthreads();  // the previous ticket's readers of sd are done
+    if (threadIdx.x == 0) sh_t = atomicAdd(sync, 1u);
+    __syncthreads();
+    const unsigned t = sh_t;
+    if (t >= total) break;
+    const int k = (int)(t / (unsigned)nitems) + 1;  // sweep 1 .. sweeps
+    const WorkItem w = items[t % (unsigned)nitems];
+    const int* src = reinterpret_cast<const int*>(d + w.sample);
+    for (int i = threadIdx.x; i < (int)(sizeof(SampleDesc) / 4); i += blockDim.x)
+      reinterpret_cast<int*>(&sd)[i] = src[i];
+    if (threadIdx.x == 0)
+      sh_ok = wait_at_least(sync + 2 + w.sample,
+                            (unsigned)(k - 1) * (unsigned)w.sample_items + extra, polls);
+    __syncthreads();
+    if (!sh_ok) {
+      if (threadIdx.x == 0) atomicExch(sync + 1, 1u);
+      break;
+    }
+    const int a = (sd.ecur0 + k - 1) & 1;
+    const float4* Ein = a ? sd.E1 : sd.E0;
+    float4* Eout = a ? sd.E0 : sd.E1;
+    const int sv = S ? S : sd.solver;
+    for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
+      const int i = w.start + q;
+      if (sv == 3) inner_c_voxel<3, true>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, i);
+      else if (sv == 2) inner_c_voxel<2, true>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, i);
+      else inner_c_voxel<1, true>(Ein, Eout, sd.R, sd.meta, sd.sa, sd.sb, i);
+    }
+    __syncthreads();  // every store of the item is issued before the release
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(sync + 2 + w.sample, 1u);
+    }
+  }
+}
+
 template <int S>
 void launch_solver_kind(int kind, int grid, int threads, const SampleDesc* d,
                         const WorkItem* items, int nitems, int round, cudaStream_t st) {
@@ -134,6 +206,28 @@ void launch_solver_kind(int kind, int grid, int threads, const SampleDesc* d,
 }
 
 }  // namespace
+
+cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
+                               int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
+                               int solver, unsigned extra, int polls) {
+  if (polls <= 0) polls = kMaxPolls;
+  cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(unsigned) * (2 + (size_t)nsamples), st);
+  if (e != cudaSuccess) return e;
+  if (nitems <= 0 || sweeps <= 0) return cudaSuccess;
+  const long long tickets = (long long)sweeps * nitems;
+  int grid = 4 * sm_count();
+  if (tickets < grid) grid = (int)tickets;
+  if (solver == 1)
+    k_batch_inner_round<1><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+  else if (solver == 2)
+    k_batch_inner_round<2><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+  else if (solver == 3)
+    k_batch_inner_round<3><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+  else
+    k_batch_inner_round<0><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, int nitems,
                          int round, int threads, int blocks, double* out, cudaStream_t st,

@@ -26,6 +26,7 @@ struct WorkItem {
   int sample;
   int start;
   int count;
+  int sample_items;  // items of the same sample in the table
 };
 
 enum { kBatchResidual = 0, kBatchInner = 1, kBatchCorrect = 2, kBatchSweep64 = 3, kBatchSumW = 4 };
@@ -37,5 +38,18 @@ enum { kBatchResidual = 0, kBatchInner = 1, kBatchCorrect = 2, kBatchSweep64 = 3
 cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, int nitems,
                          int round, int threads, int blocks, double* out, cudaStream_t st,
                          int solver = 0);
+
+// The FP32 correction sweeps 1 .. sweeps of a round (mixed form) in one
+// persistent launch walking a device tile queue: CTAs take tickets (sweep k,
+// item j) in sweep-major order from sync[0], and item j's sweep k starts once
+// every item of its sample has finished sweep k - 1 (per-sample counters
+// sync[2 + sample]).  Every wait is bounded; on expiry the CTA sets sync[1]
+// and leaves.  sync holds 2 + samples words
+// (launch_batch_round clears them itself).  extra / polls: the test hook of
+// pm_debug_round_wait (a target that is never reached, a short poll limit);
+// 0 / 0 in normal operation.
+cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
+                               int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
+                               int solver = 0, unsigned extra = 0, int polls = 0);
 
 }  // namespace pm

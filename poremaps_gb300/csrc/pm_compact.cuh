@@ -81,19 +81,27 @@ __device__ __forceinline__ void interior_xyz(int lin, const Grid& g, int& x, int
   z -= 2;
 }
 
+// Loads of the correction and residual.  COHERENT: they were written earlier
+// in the same launch by another CTA (the persistent round kernel of the
+// server), so they bypass L1 (ld.global.cg); otherwise the read-only path.
+template <bool COHERENT>
+__device__ __forceinline__ float4 ld_corr(const float4* p) {
+  return COHERENT ? __ldcg(p) : __ldg(p);
+}
+
 // e2 = L(e) + r for list position i.
-template <int SOLVER>
+template <int SOLVER, bool COHERENT = false>
 __device__ __forceinline__ void inner_c_compute(const float4* __restrict__ E,
                                                 float4* __restrict__ E2,
                                                 const float4* __restrict__ R, int i,
                                                 unsigned meta, const CompactSlots& sl) {
   const int cx = (int)(meta & 7u), cy = (int)((meta >> 3) & 7u), cz = (int)((meta >> 6) & 7u);
   auto fl = [&](int axis, int side) { return (meta >> (kMetaFluidShift + 2 * axis + side)) & 1u; };
-  const float4 C = __ldg(E + i);
-  const float4 XL = __ldg(E + sl.a.x), XR = __ldg(E + sl.a.y);
-  const float4 YL = __ldg(E + sl.a.z), YR = __ldg(E + sl.a.w);
-  const float4 ZL = __ldg(E + sl.b.x), ZR = __ldg(E + sl.b.y);
-  const float4 r = __ldg(R + i);
+  const float4 C = ld_corr<COHERENT>(E + i);
+  const float4 XL = ld_corr<COHERENT>(E + sl.a.x), XR = ld_corr<COHERENT>(E + sl.a.y);
+  const float4 YL = ld_corr<COHERENT>(E + sl.a.z), YR = ld_corr<COHERENT>(E + sl.a.w);
+  const float4 ZL = ld_corr<COHERENT>(E + sl.b.x), ZR = ld_corr<COHERENT>(E + sl.b.y);
+  const float4 r = ld_corr<COHERENT>(R + i);
   Stencil<float> s;
   // along-axis terms and the divergence read the true +-1 neighbours (0 where
   // solid; in cases 4 / 5 the solid side's slot holds the second neighbour);
@@ -127,7 +135,7 @@ __device__ __forceinline__ void inner_c_compute(const float4* __restrict__ E,
 }
 
 // One voxel of the batched kernels.
-template <int SOLVER>
+template <int SOLVER, bool COHERENT = false>
 __device__ __forceinline__ void inner_c_voxel(const float4* __restrict__ E,
                                               float4* __restrict__ E2,
                                               const float4* __restrict__ R,
@@ -137,7 +145,7 @@ __device__ __forceinline__ void inner_c_voxel(const float4* __restrict__ E,
   CompactSlots sl;
   sl.a = __ldg(sa + i);
   sl.b = __ldg(sb + i);
-  inner_c_compute<SOLVER>(E, E2, R, i, __ldg(meta + i), sl);
+  inner_c_compute<SOLVER, COHERENT>(E, E2, R, i, __ldg(meta + i), sl);
 }
 
 // r = F(x) - x in FP64 from the padded state (as dc_residual_voxel), stored

@@ -8,10 +8,11 @@
 //      admission sets the problem up on the device and runs one sweep, so every
 //      resident sample sits at the start of an it_eval block (the reference
 //      evaluates convergence after the sweeps it_eval, 2 it_eval, ...);
-//   2. runs one it_eval block for all resident samples: it_eval batched
-//      launches walking a work table of (sample, fluid-voxel run) items,
-//      captured once per change of the resident set in a CUDA graph, then a
-//      per-item sum of w;
+//   2. runs one it_eval block for all resident samples over a work table of
+//      (sample, fluid-voxel run) items: the FP64 residual, the it_eval - 1
+//      FP32 correction sweeps as one persistent kernel walking a device tile
+//      queue (or one launch per sweep), the FP64 correction and a per-item sum
+//      of w, captured once per change of the resident set in a CUDA graph;
 //   3. evaluates compute_convergence per sample (the reference's stop rule)
 //      and retires the finished ones (permeability, completion record,
 //      device memory freed) without touching the others.
@@ -22,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <deque>
 #include <mutex>
@@ -79,6 +81,9 @@ struct pm_server {
   double* d_part = nullptr;
   double* h_part = nullptr;
   size_t cap_part = 0;
+  unsigned* d_sync = nullptr;  // persistent round: ticket, error flag, per-sample counters
+  size_t cap_sync = 0;
+  unsigned* h_flag = nullptr;  // pinned copy of the error flag
   bool dirty = true;
   cudaGraphExec_t gexec = nullptr;
   int graph_kernels = 0;
@@ -90,6 +95,11 @@ struct pm_server {
 };
 
 namespace {
+
+// pm_debug_round_wait: added to every wait target of the persistent round,
+// and its poll limit (0 = the kernel's own).
+std::atomic<unsigned> g_round_extra{0};
+std::atomic<int> g_round_polls{0};
 
 double now_ms(pm_server* s) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - s->t0)
@@ -258,8 +268,10 @@ void build_items(pm_server* s, int chunk) {
     Res& r = s->res[i];
     r.item0 = (int)s->h_items.size();
     int n = r.pr->nlist;
-    for (int a = 0; a < n; a += chunk) s->h_items.push_back({(int)i, a, std::min(chunk, n - a)});
+    for (int a = 0; a < n; a += chunk)
+      s->h_items.push_back({(int)i, a, std::min(chunk, n - a), 0});
     r.nitems = (int)s->h_items.size() - r.item0;
+    for (int k = r.item0; k < r.item0 + r.nitems; ++k) s->h_items[k].sample_items = r.nitems;
   }
 }
 
@@ -267,6 +279,7 @@ pm_status upload(pm_server* s) {
   pm_status e;
   if ((e = grow(&s->d_desc, &s->cap_desc, s->h_desc.size())) != PM_OK) return e;
   if ((e = grow(&s->d_items, &s->cap_items, s->h_items.size())) != PM_OK) return e;
+  if ((e = grow(&s->d_sync, &s->cap_sync, 2 + s->h_desc.size())) != PM_OK) return e;
   if (s->h_items.size() > s->cap_part) {
     if (s->d_part) cudaFree(s->d_part);
     if (s->h_part) cudaFreeHost(s->h_part);
@@ -295,9 +308,16 @@ pm_status issue_block(pm_server* s, int* nk) {
     SCK(launch_batch(kBatchResidual, s->d_desc, s->d_items, n, 0, T, 0, nullptr, s->st,
                      s->solver));
     ++k;
-    for (int r = 1; r < s->block; ++r, ++k)
-      SCK(launch_batch(kBatchInner, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st,
-                       s->solver));
+    if (s->cfg.relaunch_sweeps) {
+      for (int r = 1; r < s->block; ++r, ++k)
+        SCK(launch_batch(kBatchInner, s->d_desc, s->d_items, n, r, T, 0, nullptr, s->st,
+                         s->solver));
+    } else if (s->block > 1) {
+      SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), s->block - 1,
+                             s->d_sync, s->st, s->solver, g_round_extra.load(),
+                             g_round_polls.load()));
+      ++k;
+    }
     SCK(launch_batch(kBatchCorrect, s->d_desc, s->d_items, n, s->block, T, 0, nullptr, s->st));
     SCK(launch_batch(kBatchSumW, s->d_desc, s->d_items, n, 0, T, 0, s->d_part, s->st));
     k += 2;
@@ -415,8 +435,14 @@ pm_status run_block(pm_server* s) {
   }
   SCK(cudaMemcpyAsync(s->h_part, s->d_part, s->h_items.size() * sizeof(double),
                       cudaMemcpyDeviceToHost, s->st));
+  const bool round = mixed(s) && !s->cfg.relaunch_sweeps && s->block > 1;
+  if (round)
+    SCK(cudaMemcpyAsync(s->h_flag, s->d_sync + 1, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                        s->st));
   SCK(cudaEventRecord(s->e1, s->st));
   SCK(cudaStreamSynchronize(s->st));
+  if (round && *s->h_flag)
+    return set_error(PM_ERR_CUDA, "batched round: a wait of the persistent sweep kernel timed out");
   float ms = 0.f;
   SCK(cudaEventElapsedTime(&ms, s->e0, s->e1));
   s->busy_ms += ms;
@@ -481,7 +507,8 @@ pm_status pm_server_create(const pm_server_config* cfg, pm_server** out) {
   s->budget = s->cfg.hbm_budget_bytes ? s->cfg.hbm_budget_bytes : (size_t)(0.8 * (double)fr);
   if ((e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&s->e0)) != cudaSuccess ||
-      (e = cudaEventCreate(&s->e1)) != cudaSuccess) {
+      (e = cudaEventCreate(&s->e1)) != cudaSuccess ||
+      (e = cudaMallocHost((void**)&s->h_flag, sizeof(unsigned))) != cudaSuccess) {
     pm_server_destroy(s);
     return cuda_error(e, "server stream/events");
   }
@@ -498,7 +525,9 @@ pm_status pm_server_destroy(pm_server* s) {
   cudaFree(s->d_desc);
   cudaFree(s->d_items);
   cudaFree(s->d_part);
+  cudaFree(s->d_sync);
   if (s->h_part) cudaFreeHost(s->h_part);
+  if (s->h_flag) cudaFreeHost(s->h_flag);
   if (s->e0) cudaEventDestroy(s->e0);
   if (s->e1) cudaEventDestroy(s->e1);
   if (s->st) cudaStreamDestroy(s->st);
@@ -566,6 +595,13 @@ pm_status pm_server_stats(pm_server* s, double* busy_ms, double* wall_ms, uint64
 }
 
 double pm_server_clock_ms(pm_server* s) { return s ? now_ms(s) : 0.0; }
+
+pm_status pm_debug_round_wait(unsigned extra, int polls) {
+  if (polls < 0) return set_error(PM_ERR_INVALID, "polls must be >= 0");
+  g_round_extra.store(extra);
+  g_round_polls.store(polls);
+  return PM_OK;
+}
 
 pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* bytes) {
   if (!s || !p || !bytes) return set_error(PM_ERR_INVALID, "bad arguments");

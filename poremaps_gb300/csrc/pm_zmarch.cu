@@ -78,7 +78,7 @@ struct Maps {
 template <class T, int SOLVER>
 __global__ void __launch_bounds__(T::THREADS)
     k_zmarch_inner(const __grid_constant__ Maps maps, float4* E2, Grid g, int zchunk,
-                   long long budget, int* err) {
+                   long long budget, int* err, int fail_first) {
   constexpr int TX = T::TX, TY = T::TY, HX = T::HX, THREADS = T::THREADS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem<T>& S = *reinterpret_cast<Smem<T>*>(smem_raw);
@@ -118,7 +118,9 @@ __global__ void __launch_bounds__(T::THREADS)
   }
   int issued = min(D + 1, L);
   int waited = 0;  // groups whose barrier phase every thread has observed
-  bool ok = __syncthreads_and(mbar_wait(&S.bar_pro, 0, budget));
+  // fail_first (test hook): the first wait reports a timeout without waiting,
+  // which exercises the failure path below with real copies in flight
+  bool ok = __syncthreads_and(fail_first ? false : mbar_wait(&S.bar_pro, 0, budget));
 
   const int tx = threadIdx.x % (TX / 2), ty = threadIdx.x / (TX / 2);
   const int yp = by * TY + ty;  // interior y
@@ -320,21 +322,27 @@ void zmarch_destroy(ZmarchPlan* pl) {
   delete pl;
 }
 
+// pm_debug_tma_fail: the next z-march launches report a timed-out first wait.
+static std::atomic<int> g_tma_fail{0};
+
 template <class T>
 static void launch_t(const ZmarchPlan* pl, int src, float4* E2, const Grid& g, int solver,
                      cudaStream_t st) {
   const long long budget = 4000000000LL;  // ~2 s at 2 GHz per wait
   const size_t sm = sizeof(Smem<T>);
+  const int ff = g_tma_fail.load();
   if (solver == 3)
     k_zmarch_inner<T, 3><<<pl->grid, T::THREADS, sm, st>>>(pl->maps[src], E2, g, pl->zchunk,
-                                                          budget, pl->err);
+                                                          budget, pl->err, ff);
   else if (solver == 2)
     k_zmarch_inner<T, 2><<<pl->grid, T::THREADS, sm, st>>>(pl->maps[src], E2, g, pl->zchunk,
-                                                          budget, pl->err);
+                                                          budget, pl->err, ff);
   else
     k_zmarch_inner<T, 1><<<pl->grid, T::THREADS, sm, st>>>(pl->maps[src], E2, g, pl->zchunk,
-                                                          budget, pl->err);
+                                                          budget, pl->err, ff);
 }
+
+void zmarch_debug_fail(int on) { g_tma_fail.store(on ? 1 : 0); }
 
 cudaError_t zmarch_inner(const ZmarchPlan* pl, int src, float4* E2, const Grid& g, int solver,
                          cudaStream_t st) {

@@ -20,5 +20,8 @@ cudaError_t zmarch_inner(const ZmarchPlan* pl, int src, float4* E2, const Grid& 
                          cudaStream_t st);
 // Device int set to 1 when a pipeline wait timed out.
 int* zmarch_error_flag(const ZmarchPlan* pl);
+// Test hook: while on, every launch reports its first wait as timed out
+// without waiting (the failure path then drains the CTA's copies in flight).
+void zmarch_debug_fail(int on);
 
 }  // namespace pm

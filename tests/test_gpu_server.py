@@ -32,10 +32,10 @@ def samples(n=6, seed=0):
 
 
 def run_server(geoms, precision="mixed", use_graphs=1, autotune=0, budget=0, kw=None,
-               submit_later=()):
+               submit_later=(), relaunch_sweeps=0):
     kw = dict(KW, **(kw or {}))
     s = pm.Server(precision=precision, use_graphs=use_graphs, autotune=autotune,
-                  hbm_budget_bytes=budget)
+                  hbm_budget_bytes=budget, relaunch_sweeps=relaunch_sweeps)
     tickets = {}
     for i, g in enumerate(geoms):
         if i not in submit_later:
@@ -328,3 +328,42 @@ def test_allocation_failure_is_reported_and_recovered():
     s.close()
     assert res[0].status == pm.PM_ERR_NOMEM
     assert res[1].status == 0 and res[1].result.wk33 == ref.wk33
+
+
+@pytest.mark.parametrize("use_graphs", [1, 0])
+def test_persistent_round_equals_one_launch_per_sweep(use_graphs):
+    """The round's FP32 sweeps as one persistent kernel walking the tile
+    queue give the same fields as one launch per sweep, bit for bit, with
+    samples of very different sizes resident together."""
+    geoms = samples(5, seed=12) + [synth.sphere_pack((40, 36, 44), rmin=1.5, rmax=3.0,
+                                                     solid_fraction=0.55, seed=13)]
+    a = run_server(geoms, use_graphs=use_graphs, relaunch_sweeps=0)
+    b = run_server(geoms, use_graphs=use_graphs, relaunch_sweeps=1)
+    for i in range(len(geoms)):
+        assert a[i].status == 0 and b[i].status == 0
+        assert a[i].result.iterations == b[i].result.iterations
+        for f in ("wk13", "wk23", "wk33", "wmax_velz"):
+            assert getattr(a[i].result, f) == getattr(b[i].result, f), (i, f)
+
+
+def test_round_wait_that_runs_out_reports_an_error():
+    """A wait of the persistent sweep kernel that can never be satisfied
+    (test hook) runs out after its poll limit: the kernel sets its error flag
+    and returns, pm_server_step reports PM_ERR_CUDA, and the device stays
+    usable -- a new server then solves the same samples normally."""
+    geoms = samples(2, seed=14)
+    pm.debug_round_wait(1 << 20, 2048)
+    try:
+        s = pm.Server(precision="mixed")
+        for g in geoms:
+            s.submit(g, **KW)
+        with pytest.raises(pm.PMError) as ei:
+            for _ in range(5):
+                s.step()
+        assert ei.value.status == 3 and "timed out" in str(ei.value)
+        s.close()
+    finally:
+        pm.debug_round_wait(0, 0)
+    res = run_server(geoms)
+    for i, g in enumerate(geoms):
+        assert res[i].status == 0 and res[i].result.wk33 == single(g).wk33

@@ -93,3 +93,33 @@ def test_compact_store_reductions_mid_block(bc, di):
             conv, perm = p.convergence()
             res.append((k.wk13, k.wk23, k.wk33, k.k33, k.wmax_velz, conv, perm))
     assert res[0] == res[1] == res[2]
+
+
+@pytest.mark.parametrize("kernel", [0, 3])
+def test_zmarch_wait_timeout_path(kernel):
+    """The z-march sweep's failure path: with the test hook every CTA treats
+    its first pipeline wait as timed out, sets the error flag and waits for
+    its copies in flight before it returns.  The sweep reports PM_ERR_CUDA;
+    afterwards the same problem, reset, sweeps normally and gives the
+    fluid-list kernel's fields bit for bit."""
+    g = synth.random_solid((24, 20, 30), 0.3, 41)
+    kw = dict(boundary_method=0, solving_algorithm=2, order="jacobi", precision="mixed",
+              mixed_inner=40)
+    with pm.Problem(g, None, kernel=kernel, **kw) as p:
+        p.iterate(3)
+        pm.debug_tma_fail(True)
+        try:
+            with pytest.raises(pm.PMError) as ei:
+                p.iterate(1)
+                p.fields()  # synchronises; the flag is read there at the latest
+        finally:
+            pm.debug_tma_fail(False)
+        assert ei.value.status == 3 and "timed out" in str(ei.value)
+        p.reset()
+        p.iterate(57)
+        got = p.fields()
+    with pm.Problem(g, None, kernel=1, **kw) as p:
+        p.iterate(57)
+        want = p.fields()
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
