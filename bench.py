@@ -74,7 +74,9 @@ def parse():
                          "rounding floor of conv)")
     ap.add_argument("--write-traffic", default=None, metavar="NCU_CSV",
                     help="write the traffic record of --kernel/--brick from an ncu CSV and exit")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--write-fp64-record", default=None, metavar="NCU_CSV",
+                    help="write the FP64-pipe record of the FP64 Jacobi sweep from an ncu CSV")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "steps"], default=None,
                     help="run two it_eval blocks of one resident problem and exit (a small, "
                          "self-contained case for ncu captures)")
     return ap.parse_args()
@@ -324,6 +326,7 @@ def run_gpu(args):
         forms["fp64"] = {"glups": glups64, "fluid_glups": glups64 * phi, "ms_per_step": ms_64,
                          "sweep_kernel_ms": k64,
                          "hbm_frac_of_measured": nvox * ALGO_BYTES_FP64 / (k64 * 1e-3) / 1e9 / peak,
+                         "fp64_pipe": fp64_pipe_record(args.size, k64),
                          "note": "FP64 sweeps are bound by the FP64 pipe of GB300, not by HBM"}
         for p in probs_64:
             p.close()
@@ -440,6 +443,84 @@ KERNEL_SOURCES = ["poremaps_gb300/csrc/pm_fast.cu", "poremaps_gb300/csrc/pm_comp
                   "poremaps_gb300/csrc/pm_internal.h"]
 
 
+FP64_SOURCES = ["poremaps_gb300/csrc/pm_fast.cu", "poremaps_gb300/csrc/pm_stencil.cuh",
+                "poremaps_gb300/csrc/pm_internal.h"]
+
+
+def _sources_sha(files):
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in files:
+        h.update(open(os.path.join(ROOT, f), "rb").read())
+    return h.hexdigest()
+
+
+def _ncu_rows(csv_path, kname):
+    """(launch id -> {metric: value}) of the launches of kernel kname in an
+    ncu --csv log."""
+    import csv
+
+    with open(csv_path) as f:
+        rows = [r for r in csv.reader(f) if len(r) > 10]
+    head = rows[0]
+    ci = {n: head.index(n) for n in ("ID", "Kernel Name", "Metric Name", "Metric Unit",
+                                     "Metric Value")}
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "ns": 1e-3, "us": 1.0,
+             "ms": 1e3, "%": 1.0, "inst": 1.0, "": 1.0}
+    per = {}
+    for r in rows[1:]:
+        if kname not in r[ci["Kernel Name"]]:
+            continue
+        v = float(r[ci["Metric Value"]].replace(",", "")) * scale.get(r[ci["Metric Unit"]], 1.0)
+        per.setdefault(r[ci["ID"]], {})[r[ci["Metric Name"]]] = v
+    return per
+
+
+def write_fp64_record(csv_path, size):
+    """FP64-pipe record of the FP64 Jacobi sweep (k_sweep64_pf) from an ncu CSV
+    of `bench.py --profile-case fp64` with the metrics
+    sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active,
+    sm__inst_executed_pipe_fp64.sum and gpu__time_duration.sum."""
+    per = _ncu_rows(csv_path, "k_sweep64_pf")
+    if not per:
+        raise SystemExit(f"no k_sweep64_pf launches in {csv_path}")
+    first = per[sorted(per, key=int)[0]]  # the Jacobi sweep's launches come first
+    out = {"kernel": "k_sweep64_pf", "workload": f"{size}^3 sphere pack (bench default), FP64 "
+                                                "Jacobi, one rotated problem",
+           "fp64_pipe_active_pct": first["sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active"],
+           "fp64_warp_instructions": first["sm__inst_executed_pipe_fp64.sum"],
+           "duration_us": first["gpu__time_duration.sum"],
+           "sources": FP64_SOURCES, "sources_sha256": _sources_sha(FP64_SOURCES),
+           "source": "ncu --metrics sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active,"
+                     "sm__inst_executed_pipe_fp64.sum,gpu__time_duration.sum --clock-control none "
+                     "-k regex:k_sweep64_pf -s 2 -c 1 python bench.py --profile-case fp64; "
+                     "one launch, cold caches"}
+    path = os.path.join(ROOT, "profiles", f"k_sweep64_pf_sphere{size}_fp64pipe.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    print(json.dumps(out))
+    return 0
+
+
+def fp64_pipe_record(size, kernel_ms):
+    """The FP64 Jacobi sweep's FP64-pipe utilisation: measured by ncu on one
+    cold launch, and scaled to the warm event time of this run (the pipe does
+    the same work in less time when the caches are warm)."""
+    path = os.path.join(ROOT, "profiles", f"k_sweep64_pf_sphere{size}_fp64pipe.json")
+    if not os.path.exists(path):
+        return None
+    t = json.load(open(path))
+    if t.get("sources") != FP64_SOURCES or t.get("sources_sha256") != _sources_sha(FP64_SOURCES):
+        return {"stale": "kernel sources changed since the capture"}
+    return {"active_pct_ncu_cold": t["fp64_pipe_active_pct"],
+            "active_frac_at_event_time": t["fp64_pipe_active_pct"] / 100.0 *
+            (t["duration_us"] * 1e-3) / kernel_ms,
+            "fp64_warp_instructions_per_sweep": t["fp64_warp_instructions"],
+            "source": t["source"]}
+
+
 def write_traffic(csv_path, kid, brick, size):
     """Turn an ncu CSV of the chosen correction sweep (the metrics
     dram__bytes_read.sum and dram__bytes_write.sum, launches of
@@ -502,6 +583,19 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
 def run_profile_case(args):
     import poremaps_gb300 as pm
 
+    if args.profile_case == "steps":
+        # the headline's timed loop alone: the three rotated mixed problems,
+        # --warmup + --steps concurrent it_eval blocks (for a launch list)
+        g, rots = workload(args.size)
+        probs = [pm.Problem(r, None, precision="mixed", solving_algorithm=3, boundary_method=0,
+                            voxel_size=1e-5, eps=1e-6, it_eval=SWEEPS_PER_BLOCK,
+                            it_write=SWEEPS_PER_BLOCK, order="jacobi") for r in rots]
+        perm = [0.0, 0.0, 0.0]
+        for _ in range(args.warmup + args.steps):
+            _, _, perm = pm.block_group_timed(probs, SWEEPS_PER_BLOCK, True, perm)
+        for p in probs:
+            p.close()
+        return 0
     if args.workload == "c3":
         # the c3 medium at --size (a few GB on the device at 256^3): two
         # it_eval blocks of the mixed form, or of FP64 Jacobi and red-black
@@ -875,6 +969,8 @@ def main():
     args = parse()
     if args.write_traffic:
         return write_traffic(args.write_traffic, args.kernel, args.brick, args.size)
+    if args.write_fp64_record:
+        return write_fp64_record(args.write_fp64_record, args.size)
     if args.profile_case:
         return run_profile_case(args)
     if args.workload == "c3":

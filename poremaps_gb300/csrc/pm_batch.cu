@@ -209,13 +209,15 @@ void launch_solver_kind(int kind, int grid, int threads, const SampleDesc* d,
 
 cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
                                int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
-                               int solver, unsigned extra, int polls) {
+                               int solver, unsigned extra, int polls, int ctas_per_sm) {
   if (polls <= 0) polls = kMaxPolls;
+  if (ctas_per_sm < 1) ctas_per_sm = 1;
+  if (ctas_per_sm > 4) ctas_per_sm = 4;
   cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(unsigned) * (2 + (size_t)nsamples), st);
   if (e != cudaSuccess) return e;
   if (nitems <= 0 || sweeps <= 0) return cudaSuccess;
   const long long tickets = (long long)sweeps * nitems;
-  int grid = 4 * sm_count();
+  int grid = ctas_per_sm * sm_count();
   if (tickets < grid) grid = (int)tickets;
   if (solver == 1)
     k_batch_inner_round<1><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);

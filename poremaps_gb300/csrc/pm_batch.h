@@ -12,7 +12,7 @@ struct SampleDesc {
   float4 *E0, *E1, *R;    // FP32 correction (ping-pong) and residual: the compact store,
                           // one float4 (u, v, w, p) per fluid-list position and a zero slot
   const uint8_t* codes;
-  const unsigned* meta;   // compact store: code and plane flags per list position
+  const unsigned* meta;   // compact store: cases, flags per list position
   const int4* sa;         // compact store: x L, x R, y L, y R neighbour positions
   const int2* sb;         // compact store: z L, z R neighbour positions
   const int* list;
@@ -48,8 +48,11 @@ cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, i
 // (launch_batch_round clears them itself).  extra / polls: the test hook of
 // pm_debug_round_wait (a target that is never reached, a short poll limit);
 // 0 / 0 in normal operation.
+// ctas_per_sm: resident CTAs of 256 threads per SM the persistent grid holds
+// (1..4; the server's autotuner picks it).
 cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
                                int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
-                               int solver = 0, unsigned extra = 0, int polls = 0);
+                               int solver = 0, unsigned extra = 0, int polls = 0,
+                               int ctas_per_sm = 4);
 
 }  // namespace pm

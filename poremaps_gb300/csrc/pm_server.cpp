@@ -26,7 +26,9 @@
 #include <atomic>
 #include <chrono>
 #include <deque>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/poremaps.h"
@@ -88,6 +90,7 @@ struct pm_server {
   cudaGraphExec_t gexec = nullptr;
   int graph_kernels = 0;
   int threads = 256, chunk = 8192;
+  int round_ctas = 4;  // CTAs per SM of the persistent round kernel
   int solver = 0;  // the solver every resident sample uses, 0 when they differ
   long long tuned_for = -1;
   double busy_ms = 0.0;
@@ -315,7 +318,7 @@ pm_status issue_block(pm_server* s, int* nk) {
     } else if (s->block > 1) {
       SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), s->block - 1,
                              s->d_sync, s->st, s->solver, g_round_extra.load(),
-                             g_round_polls.load()));
+                             g_round_polls.load(), s->round_ctas));
       ++k;
     }
     SCK(launch_batch(kBatchCorrect, s->d_desc, s->d_items, n, s->block, T, 0, nullptr, s->st));
@@ -332,39 +335,102 @@ pm_status issue_block(pm_server* s, int* nk) {
   return PM_OK;
 }
 
-// Time the main batched sweep for a few (threads, chunk) shapes on the current
-// resident set and keep the fastest.  Safe at a block boundary: the timed
-// launches only write buffers the next block's first sweep rewrites.
+// Launch shape of the batched sweeps, timed on the current resident set:
+// the work-item size (voxels per tile of the queue) and, for the persistent
+// round, the CTAs per SM of its grid (a 3-sweep round per candidate); for
+// one launch per sweep, the threads per block.  Decisions are kept per size
+// class (precision, launch form, solver, log2 of the resident fluid voxels,
+// log2 of the resident samples), so a stream whose resident set keeps its
+// size tunes once.  Safe at a block boundary: the timed launches only write
+// correction buffers the next block's residual and first sweep rewrite.
+struct TuneKey {
+  int mixed, persistent, solver, fluid_class, samples_class;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(mixed, persistent, solver, fluid_class, samples_class) <
+           std::tie(o.mixed, o.persistent, o.solver, o.fluid_class, o.samples_class);
+  }
+};
+struct TuneVal {
+  int threads, chunk, ctas;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tuned;
+
+int log2_class(long long v) {
+  int c = 0;
+  while (v > 1) { v >>= 1; ++c; }
+  return c;
+}
+
 pm_status autotune(pm_server* s) {
   static const int kThreads[] = {128, 256, 512};
   static const int kChunks[] = {2048, 8192, 32768};
+  static const int kCtas[] = {2, 3, 4};
   long long total = 0;
   for (auto& r : s->res) total += r.pr->nlist;
   if (s->tuned_for > 0 && total < 4 * s->tuned_for && 4 * total > s->tuned_for) return PM_OK;
+  const bool persistent = mixed(s) && !s->cfg.relaunch_sweeps && s->block > 1;
+  const TuneKey key{mixed(s) ? 1 : 0, persistent ? 1 : 0, s->solver, log2_class(total),
+                    log2_class((long long)s->res.size())};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      s->threads = it->second.threads;
+      s->chunk = it->second.chunk;
+      s->round_ctas = it->second.ctas;
+      s->tuned_for = total;
+      return PM_OK;
+    }
+  }
   float best = 1e30f;
-  int bt = s->threads, bc = s->chunk;
+  int bt = s->threads, bc = s->chunk, bm = s->round_ctas;
   const int kind = mixed(s) ? kBatchInner : kBatchSweep64;
+  auto time_it = [&](auto&& issue, float* ms) -> pm_status {
+    pm_status e = issue();  // warm-up
+    if (e != PM_OK) return e;
+    SCK(cudaEventRecord(s->e0, s->st));
+    for (int i = 0; i < 3; ++i)
+      if ((e = issue()) != PM_OK) return e;
+    SCK(cudaEventRecord(s->e1, s->st));
+    SCK(cudaEventSynchronize(s->e1));
+    SCK(cudaEventElapsedTime(ms, s->e0, s->e1));
+    return PM_OK;
+  };
   for (int c : kChunks) {
     build_items(s, c);
     pm_status e = upload(s);
     if (e != PM_OK) return e;
-    for (int t : kThreads) {
-      SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
-                       s->st, s->solver));
-      SCK(cudaEventRecord(s->e0, s->st));
-      for (int i = 0; i < 3; ++i)
-        SCK(launch_batch(kind, s->d_desc, s->d_items, (int)s->h_items.size(), 1, t, 0, nullptr,
-                         s->st, s->solver));
-      SCK(cudaEventRecord(s->e1, s->st));
-      SCK(cudaEventSynchronize(s->e1));
-      float ms = 0.f;
-      SCK(cudaEventElapsedTime(&ms, s->e0, s->e1));
-      if (ms < best) { best = ms; bt = t; bc = c; }
+    const int n = (int)s->h_items.size();
+    if (persistent) {
+      for (int m : kCtas) {
+        float ms = 0.f;
+        e = time_it([&]() -> pm_status {
+          SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), 3, s->d_sync,
+                                 s->st, s->solver, 0, 0, m));
+          return PM_OK;
+        }, &ms);
+        if (e != PM_OK) return e;
+        if (ms < best) { best = ms; bc = c; bm = m; }
+      }
+    } else {
+      for (int t : kThreads) {
+        float ms = 0.f;
+        e = time_it([&]() -> pm_status {
+          SCK(launch_batch(kind, s->d_desc, s->d_items, n, 1, t, 0, nullptr, s->st, s->solver));
+          return PM_OK;
+        }, &ms);
+        if (e != PM_OK) return e;
+        if (ms < best) { best = ms; bt = t; bc = c; }
+      }
     }
   }
   s->threads = bt;
   s->chunk = bc;
+  s->round_ctas = bm;
   s->tuned_for = total;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = {bt, bc, bm};
   return PM_OK;
 }
 

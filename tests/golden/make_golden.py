@@ -3,7 +3,7 @@ reference POREMAPS program itself (its own src/*.cc, built unmodified against
 the MPI shim by `make -C oracle ref`) on small seeded geometries.
 
 Run in a container where the reference sources exist:
-    make -C oracle ref && python tests/golden/make_golden.py [--slow]
+    make -C oracle ref REF_SRC=<reference checkout>/src && python tests/golden/make_golden.py [--slow]
 
 Each case stores the log text (TPS column blanked: it is wall-clock time), the
 SHA-256 of every field file the program writes, and for the smallest cases
