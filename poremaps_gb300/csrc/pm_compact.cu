@@ -1,5 +1,5 @@
 // Compact correction store of the mixed-precision form (correction-sweep
-// kernel 8).
+// kernels 8 and 9, and the server's batched sweeps).
 //
 // The FP32 correction e and residual r hold one float4 (u, v, w, p) per
 // fluid voxel, at the voxel's position in the lexicographic fluid list,
