@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256, 2) k_dc_residual_c(Fields<double> X, floa
                                                         float4* E, const uint8_t* codes,
                                                         const int* list, int nlist, Grid g) {
   __shared__ double ctab[16];
-  fill_centre_table(ctab);
+  fill_centre_table<SOLVER>(ctab);
   __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;

@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(256) k_sweep64_fast(Fields<double> A, Fields<d
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
   __shared__ double ctab[16];
-  fill_centre_table(ctab);
+  fill_centre_table<SOLVER>(ctab);
   __syncthreads();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x)
     sweep64_voxel<SOLVER, PHASE, false>(A, B, codes, g, list[q], ctab);
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep64_pf(Fields<double> A, Fields<
                                                       const uint8_t* codes, const int* list,
                                                       int nlist, Grid g) {
   __shared__ double ctab[16];
-  fill_centre_table(ctab);
+  fill_centre_table<SOLVER>(ctab);
   __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256, 2) k_dc_residual(Fields<double> X, float4
                                                       int nlist, Grid g) {
   // persistent, next list entry prefetched (as the FP64 sweeps)
   __shared__ double ctab[16];
-  fill_centre_table(ctab);
+  fill_centre_table<SOLVER>(ctab);
   __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;

@@ -5,9 +5,11 @@
 //     units that use it are compiled with -fmad=false), bit-identical to the
 //     reference CPU program;
 //   * update_fast: the same linear map regrouped into a coefficient form with
-//     FMAs (about 39 floating-point instructions per fluid voxel instead of
-//     ~70 plus three divisions), used by the FP64 fast sweeps and by the FP32
-//     correction sweeps of the mixed-precision form.
+//     FMAs (31 FP64 instructions per fluid voxel in FP64, where the relaxation
+//     is folded into the coefficients and the centre coefficient comes from a
+//     16-entry table; about 39 in FP32; instead of ~70 plus three divisions),
+//     used by the FP64 fast sweeps, the FP64 residual and the FP32 correction
+//     sweeps of the mixed-precision form.
 #pragma once
 
 #include "pm_internal.h"
@@ -136,18 +138,74 @@ __device__ __forceinline__ int case_group(int cs) {
   return cs == 1 ? 0 : (cs <= 3 ? 1 : (cs <= 5 ? 2 : 3));
 }
 
-// Centre coefficients (-2 + a1) + a2 of a velocity's two cross stencils for
-// the 4 x 4 case groups, with exactly the arithmetic of vel_fast (the table
-// holds the same doubles it would compute).  Filled once per CTA by the FP64
-// kernels, whose FP64 pipe is their bound: three shared-memory reads replace
-// six FP64 additions per voxel.
+// Centre coefficient a of a case group (the FP64 form's centre table is built
+// from it: see centre64).
 __device__ __forceinline__ double group_a(int g) {
   return g == 0 ? -8.0 : (g == 1 ? -16.0 / 3.0 : (g == 2 ? -5.0 : -2.0));
 }
 
+// FP64 form: the relaxation of the solver is folded into the coefficients,
+// so a new velocity is one FMA chain over its nine stencil values
+//   v' = Cc c + K' (am + ap + cA1 A1 + cB1 B1 + cA2 A2 + cB2 B2) - dt' (pc - pm)
+// with K' = dt/Re, dt' = dt (solvers 1, 2) or K' = omega dt/Re, dt' = omega dt
+// (solver 3, whose update is (1 - omega) c + omega dt (-dp + f/Re)), and the
+// centre coefficient Cc = 1 + K' ctr (solvers 1, 2) or (1 - omega) + K' ctr
+// (solver 3), ctr = -2 + a1 + a2.  -dt' pc is shared by the three velocities.
+// 31 FP64 instructions per fluid voxel instead of 36 (SOR) / 33: GB300's
+// FP64 pipe (1/64 of the FP32 rate) bounds the FP64 sweeps.
+template <int SOLVER>
+struct Relax64 {
+  static constexpr double K = SOLVER == 3 ? kDt / kRe * kOmega : kDt / kRe;
+  static constexpr double Dt = SOLVER == 3 ? kDt * kOmega : kDt;
+  static constexpr double Base = SOLVER == 3 ? 1.0 - kOmega : 1.0;
+};
+
+template <int SOLVER>
+__device__ __forceinline__ double centre64(int g1, int g2) {
+  const double ctr = (-2.0 + group_a(g1)) + group_a(g2);
+  return __fma_rn(Relax64<SOLVER>::K, ctr, Relax64<SOLVER>::Base);
+}
+
+template <int SOLVER>
 __device__ __forceinline__ void fill_centre_table(double* tab) {
-  for (int i = threadIdx.x; i < 16; i += blockDim.x)
-    tab[i] = (-2.0 + group_a(i >> 2)) + group_a(i & 3);
+  for (int i = threadIdx.x; i < 16; i += blockDim.x) tab[i] = centre64<SOLVER>(i >> 2, i & 3);
+}
+
+// Off-centre coefficients of a wall stencil of case cs times K' (see case_coef).
+template <int SOLVER>
+__device__ __forceinline__ void case_coef64(int cs, double& cA, double& cB) {
+  constexpr double K = Relax64<SOLVER>::K;
+  switch (cs) {
+    case 1: cA = 0.0; cB = 0.0; break;
+    case 2: case 3: cA = K * (8.0 / 3.0); cB = 0.0; break;
+    case 4: case 5: cA = K * 2.0; cB = K * -0.2; break;
+    default: cA = K; cB = K; break;
+  }
+}
+
+template <int SOLVER>
+__device__ __forceinline__ double vel64(double c, double am, double ap, int cs1, double ll1,
+                                        double l1, double r1, double rr1, int cs2, double ll2,
+                                        double l2, double r2, double rr2, double pm, double P,
+                                        bool lsolid, const double* ctab) {
+  double cA1, cB1, cA2, cB2, A1, B1, A2, B2;
+  case_coef64<SOLVER>(cs1, cA1, cB1);
+  case_coef64<SOLVER>(cs2, cA2, cB2);
+  case_pick<double>(cs1, ll1, l1, r1, rr1, A1, B1);
+  case_pick<double>(cs2, ll2, l2, r2, rr2, A2, B2);
+  constexpr double K = Relax64<SOLVER>::K;
+  const double Cc = ctab ? ctab[case_group(cs1) * 4 + case_group(cs2)]
+                         : centre64<SOLVER>(case_group(cs1), case_group(cs2));
+  // no pressure difference where the left neighbour is solid
+  double t = lsolid ? 0.0 : fma(Relax64<SOLVER>::Dt, pm, P);
+  t = fma(Cc, c, t);
+  t = fma(K, am, t);
+  t = fma(K, ap, t);
+  t = fma(cA1, A1, t);
+  t = fma(cB1, B1, t);
+  t = fma(cA2, A2, t);
+  t = fma(cB2, B2, t);
+  return (SOLVER != 3 && lsolid) ? 0.0 : t;
 }
 
 template <typename T, int SOLVER>
@@ -182,6 +240,20 @@ __device__ __forceinline__ void update_fast_cases(const Stencil<T>& s, int cx, i
                                                   T& un, T& vn, T& wn, T& pn,
                                                   const T* ctab = nullptr) {
   const bool lx = left_solid(cx), ly = left_solid(cy), lz = left_solid(cz);
+  if constexpr (sizeof(T) == 8) {
+    const double P = -Relax64<SOLVER>::Dt * s.pc;
+    double d0 = 0.0;
+    if (SOLVER == 1) d0 = ((s.wzp - s.wc) + (s.vyp - s.vc)) + (s.uxp - s.uc);
+    un = vel64<SOLVER>(s.uc, s.uxm, s.uxp, cy, s.uymm, s.uym, s.uyp, s.uypp, cz, s.uzmm, s.uzm,
+                       s.uzp, s.uzpp, s.pxm, P, lx, ctab);
+    vn = vel64<SOLVER>(s.vc, s.vym, s.vyp, cx, s.vxmm, s.vxm, s.vxp, s.vxpp, cz, s.vzmm, s.vzm,
+                       s.vzp, s.vzpp, s.pym, P, ly, ctab);
+    wn = vel64<SOLVER>(s.wc, s.wzm, s.wzp, cx, s.wxmm, s.wxm, s.wxp, s.wxpp, cy, s.wymm, s.wym,
+                       s.wyp, s.wypp, s.pzm, P, lz, ctab);
+    const double dv = (SOLVER == 1) ? d0 : ((s.wzp - wn) + (s.vyp - vn)) + (s.uxp - un);
+    pn = fma(-kC2 * kDt, dv, s.pc);
+    return;
+  }
   const T dpx = lx ? T(0) : s.pc - s.pxm;
   const T dpy = ly ? T(0) : s.pc - s.pym;
   const T dpz = lz ? T(0) : s.pc - s.pzm;
@@ -228,8 +300,11 @@ __device__ __forceinline__ void gather(Stencil<T>& s, const Fields<T>& A, const 
   const long long sx = 1, sy = px, sz = pl;
   // PHASE 2 (black): interior +-1 neighbours are red and already updated (in
   // B); every other read (centre, +-2, halos) is the previous iterate (A).
+  // (one load from a selected base: the red values this pass reads from B are
+  // not written by it)
   auto P = [&](const T* a, const T* b, long long o, bool interior) -> T {
-    return (PHASE == 2 && interior) ? b[c + o] : ldA(a + c + o, NC);
+    if (PHASE == 2) return ldA((interior ? b : a) + c + o, NC);
+    return ldA(a + c + o, NC);
   };
   const bool ixm = x - 1 >= 2, ixp = x + 1 <= g.NX - 3;
   const bool iym = y - 1 >= 2, iyp = y + 1 <= g.NY - 3;
