@@ -577,7 +577,9 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
            8: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
                                "3 blocks/SM"),
            9: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
-                               "4 blocks/SM")}
+                               "4 blocks/SM"),
+           10: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
+                                "5 blocks/SM, no slot prefetch")}
 
 
 def run_profile_case(args):

@@ -97,18 +97,20 @@ typedef struct {
   int write_log;                /* 1: append the reference log rows to log_file_name */
   int mixed_inner;              /* FP32 sweeps per FP64 correction (0 = it_eval) */
   int kernel;                   /* correction sweep of the mixed form: -1 autotune
-                                   (default: time the kernels 9, 8, 6, 5, 7, 2 on the
-                                   problem, keep the fastest),
+                                   (default: time the kernels 10, 9, 8, 6, 5, 7, 2 on
+                                   the problem; the first is kept unless another is
+                                   at least 5 % faster),
                                    0 TMA z-march 32x16 tiles, 3 TMA
                                    z-march 32x8 tiles, 1 fluid-list gather, 2 fluid-list
                                    gather at four blocks per SM, 4 TMA bricks (one
                                    brick + halo per CTA in shared memory), 5 / 6 / 7
                                    persistent fluid-list gather, list prefetched, at
-                                   four / three / two blocks per SM, 8 / 9 persistent
-                                   sweep over a compact store (correction and
-                                   residual of fluid voxels only, in fluid-list
+                                   four / three / two blocks per SM, 8 / 9 / 10
+                                   persistent sweep over a compact store (correction
+                                   and residual of fluid voxels only, in fluid-list
                                    order, six neighbour positions per voxel) at
-                                   three / four blocks per SM */
+                                   three / four blocks per SM with the next
+                                   positions prefetched, five blocks per SM without */
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */

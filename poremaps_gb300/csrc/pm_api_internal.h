@@ -104,7 +104,7 @@ struct pm_problem {
   pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
   pm::BrickPlan* bp = nullptr;   // TMA brick plan of the mixed form
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
-  bool compact() const { return kern == 8 || kern == 9; }
+  bool compact() const { return kern == 8 || kern == 9 || kern == 10; }
   int brick[3] = {0, 0, 0};      // fluid-list order: bricks (0 = lexicographic rows)
   // state
   int cur = 0;        // FP64 state buffer holding the current iterate

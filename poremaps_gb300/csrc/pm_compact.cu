@@ -34,9 +34,14 @@ namespace pm {
 namespace {
 
 // Persistent: one wave of MINB CTAs per SM walks the list positions with a
-// grid stride; each thread loads the metadata and slots of its next position
-// before it sweeps the current one, so only the correction loads wait.
-template <int SOLVER, int MINB>
+// grid stride.  PF: each thread loads the metadata and slots of its next
+// position before it sweeps the current one, so only the correction loads
+// wait (3 or 4 CTAs per SM).  Without PF the kernel fits in 48 registers and
+// runs 5 CTAs per SM: the slot loads wait too, but 40 resident warps instead
+// of 32 hide more of the latency when several problems share the device (the
+// three rotations of the tensor: 2.75 against 2.86 ms per 100-sweep step of
+// the 128^3 sphere pack; alone both take 10.4 us).
+template <int SOLVER, int MINB, bool PF>
 __global__ void __launch_bounds__(256, MINB) k_dc_inner_c(const float4* __restrict__ E,
                                                          float4* __restrict__ E2,
                                                          const float4* __restrict__ R,
@@ -46,6 +51,10 @@ __global__ void __launch_bounds__(256, MINB) k_dc_inner_c(const float4* __restri
                                                          int nlist) {
   const int stride = gridDim.x * blockDim.x;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!PF) {
+    for (; q < nlist; q += stride) inner_c_voxel<SOLVER>(E, E2, R, meta, sa, sb, q);
+    return;
+  }
   if (q >= nlist) return;
   unsigned m = __ldg(meta + q);
   CompactSlots sl;
@@ -189,15 +198,18 @@ cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, 
   return cudaGetLastError();
 }
 
-template <int MINB>
+template <int MINB, bool PF>
 static cudaError_t inner_c_launch(const float4* e, float4* e2, const float4* r,
                                   const unsigned* meta, const int4* sa, const int2* sb,
                                   int nlist, int solver, cudaStream_t st) {
   if (nlist < 1) return cudaSuccess;
   const int blocks = grid_for(nlist, 256, MINB * sm_count());
-  if (solver == 1) k_dc_inner_c<1, MINB><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
-  else if (solver == 2) k_dc_inner_c<2, MINB><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
-  else k_dc_inner_c<3, MINB><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
+  if (solver == 1)
+    k_dc_inner_c<1, MINB, PF><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
+  else if (solver == 2)
+    k_dc_inner_c<2, MINB, PF><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
+  else
+    k_dc_inner_c<3, MINB, PF><<<blocks, 256, 0, st>>>(e, e2, r, meta, sa, sb, nlist);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -205,9 +217,10 @@ static cudaError_t inner_c_launch(const float4* e, float4* e2, const float4* r,
 cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, const unsigned* meta,
                               const int4* sa, const int2* sb, int nlist, int solver, int minb,
                               cudaStream_t st) {
-  if (minb <= 2) return inner_c_launch<2>(e, e2, r, meta, sa, sb, nlist, solver, st);
-  if (minb == 3) return inner_c_launch<3>(e, e2, r, meta, sa, sb, nlist, solver, st);
-  return inner_c_launch<4>(e, e2, r, meta, sa, sb, nlist, solver, st);
+  if (minb <= 2) return inner_c_launch<2, true>(e, e2, r, meta, sa, sb, nlist, solver, st);
+  if (minb == 3) return inner_c_launch<3, true>(e, e2, r, meta, sa, sb, nlist, solver, st);
+  if (minb == 4) return inner_c_launch<4, true>(e, e2, r, meta, sa, sb, nlist, solver, st);
+  return inner_c_launch<5, false>(e, e2, r, meta, sa, sb, nlist, solver, st);
 }
 
 cudaError_t launch_dc_residual_c(Fields<double> x, float4* r, float4* e, const uint8_t* codes,

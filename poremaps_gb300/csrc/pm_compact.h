@@ -15,7 +15,8 @@ long long compact_words(const Grid& g);
 // and the ascending lexicographic fluid list.
 cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, int nlist,
                           uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st);
-// e2 = L(e) + r (FP32), persistent with minb CTAs of 256 threads per SM.  The
+// e2 = L(e) + r (FP32), persistent with minb CTAs of 256 threads per SM (2-4:
+// next slots prefetched; 5: without the prefetch, in 48 registers).  The
 // correction buffers hold nlist + 1 entries, the last the zero slot.
 cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, const unsigned* meta,
                               const int4* sa, const int2* sb, int nlist, int solver, int minb,
