@@ -579,7 +579,11 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
            9: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
                                "4 blocks/SM"),
            10: ("k_dc_inner_c", "persistent FP32 correction sweep over the compact fluid store, "
-                                "5 blocks/SM, no slot prefetch")}
+                                "5 blocks/SM, no slot prefetch"),
+           11: ("k_dc_inner_cb", "persistent FP32 correction sweep over the compact fluid store, "
+                                 "slots staged in shared memory by bulk copies, 5 blocks/SM"),
+           12: ("k_dc_inner_cb", "persistent FP32 correction sweep over the compact fluid store, "
+                                 "slots staged in shared memory by bulk copies, 4 blocks/SM")}
 
 
 def run_profile_case(args):

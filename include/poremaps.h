@@ -110,7 +110,10 @@ typedef struct {
                                    and residual of fluid voxels only, in fluid-list
                                    order, six neighbour positions per voxel) at
                                    three / four blocks per SM with the next
-                                   positions prefetched, five blocks per SM without */
+                                   positions prefetched, five blocks per SM without,
+                                   11 / 12 the same with each chunk's positions
+                                   staged in shared memory by bulk copies at five /
+                                   four blocks per SM */
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */
@@ -328,7 +331,8 @@ pm_status pm_debug_fail_alloc(int nth);
  * after the call; 0, 0 restores normal operation.  Process-wide. */
 pm_status pm_debug_round_wait(unsigned extra, int polls);
 /* While on, every launch of the TMA z-march correction sweep (kernels 0 and 3)
- * reports its first pipeline wait as timed out without waiting: each CTA sets
+ * and of the bulk-staged compact sweep (kernels 11 and 12) reports its first
+ * pipeline wait as timed out without waiting: each CTA sets
  * the error flag, waits (bounded) for its copies in flight and returns, and
  * the sweep's caller gets PM_ERR_CUDA with the device still usable.  0 turns
  * it off.  Process-wide. */

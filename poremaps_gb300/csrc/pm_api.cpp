@@ -103,7 +103,7 @@ pm_status validate(const pm_params* p) {
     if (!none && !all)
       return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
   }
-  if (p->kernel < -1 || p->kernel > 10) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel < -1 || p->kernel > 12) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
   if (p->kernel == 4 && p->brick[0] && pm::brick_shape_of(p->brick[0], p->brick[1], p->brick[2]) < 0)
     return set_error(PM_ERR_INVALID, "kernel 4 bricks are 32x8x8, 32x8x4 or 32x4x4");
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
@@ -116,8 +116,9 @@ pm_status validate(const pm_params* p) {
 pm_status device_sync(pm_problem* pr, const char* where) {
   cudaError_t e = cudaStreamSynchronize(pr->st);
   if (e != cudaSuccess) return cuda_error(e, where);
-  int* flags[2] = {pr->zp ? zmarch_error_flag(pr->zp) : nullptr,
-                   pr->bp ? brick_error_flag(pr->bp) : nullptr};
+  int* flags[3] = {pr->zp ? zmarch_error_flag(pr->zp) : nullptr,
+                   pr->bp ? brick_error_flag(pr->bp) : nullptr,
+                   (pr->kern == 11 || pr->kern == 12) ? pr->cerr : nullptr};
   for (int* f : flags) {
     if (!f) continue;
     int flag = 0;
@@ -133,7 +134,11 @@ pm_status device_sync(pm_problem* pr, const char* where) {
 
 // The FP32 correction sweep e_out = L(e_in) + r of the mixed form.
 pm_status correction_sweep(pm_problem* pr, int src) {
-  if (pr->compact()) {
+  if (pr->kern == 11 || pr->kern == 12) {
+    CK(launch_dc_inner_cb(pr->Ec[src], pr->Ec[1 - src], pr->Rc, pr->cmeta, pr->cslot4,
+                          pr->cslot2, pr->nlist, pr->solver, pr->kern == 11 ? 5 : 4, pr->cerr,
+                          pr->st));
+  } else if (pr->compact()) {
     CK(launch_dc_inner_c(pr->Ec[src], pr->Ec[1 - src], pr->Rc, pr->cmeta, pr->cslot4,
                          pr->cslot2, pr->nlist, pr->solver, pr->kern - 5, pr->st));
   } else if (pr->zp) {
@@ -223,7 +228,9 @@ pm_status choose_fp64_shapes(pm_problem* pr) {
 // 6 and 7 persistent fluid-list gather with the list prefetched (4 / 3 / 2
 // CTAs per SM), 8, 9 and 10 persistent sweep over the compact store
 // (pm_compact.cu: fluid voxels only, six precomputed neighbour positions per
-// voxel; 3 / 4 CTAs per SM with the next positions prefetched, 5 without).
+// voxel; 3 / 4 CTAs per SM with the next positions prefetched, 5 without),
+// 11 and 12 the same sweep with each chunk's positions staged in shared
+// memory by bulk copies (5 / 4 CTAs per SM).
 // kernel < 0 times the fluid-list candidates on this problem (a few launches
 // each; the correction buffers are scratch until the first residual sweep)
 // and keeps the fastest.
@@ -249,6 +256,8 @@ void release_unused_store(pm_problem* pr) {
     cudaFree(pr->cslot2);
     cudaFree(pr->cmeta);
     cudaFree(pr->cwords);
+    cudaFree(pr->cerr);
+    pr->cerr = nullptr;
     pr->c_base = pr->Ec[0] = pr->Ec[1] = pr->Rc = nullptr;
     pr->cslot4 = nullptr;
     pr->cslot2 = nullptr;
@@ -266,7 +275,7 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     if (pr->zp) { zmarch_destroy(pr->zp); pr->zp = nullptr; }
     if (pr->bp) { brick_destroy(pr->bp); pr->bp = nullptr; }
     pr->kern = k;
-    const bool cpt = k == 8 || k == 9 || k == 10;
+    const bool cpt = k >= 8 && k <= 12;
     if (cpt) b = kLex;
     {
       int* dcount = (int*)pr->dout;
@@ -312,9 +321,9 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     release_unused_store(pr);
     return device_sync(pr, "kernel choice");
   }
-  // The TMA kernels (0, 3, 4) lose on every medium measured so far and are
-  // left to explicit choice; timing them would only lengthen the set-up of
-  // every problem.
+  // The TMA kernels (0, 3, 4) and the bulk-staged compact sweeps (11, 12)
+  // lose on every medium measured so far and are left to explicit choice;
+  // timing them would only lengthen the set-up of every problem.
   const Cand cands[] = {{10, {0, 0, 0}}, {9, {0, 0, 0}}, {8, {0, 0, 0}}, {6, {0, 0, 0}},
                         {6, {32, 8, 8}}, {5, {0, 0, 0}}, {7, {0, 0, 0}}, {2, {0, 0, 0}}};
   const int nc = 8;
@@ -638,12 +647,13 @@ size_t problem_device_bytes(const pm_params* p) {
   size_t b = (size_t)g.allocc + 4 * (size_t)g.nvox + 2 * 4 * 8 * (size_t)g.alloc64;
   // the padded correction store, the compact one (fluid voxels <= voxels), or
   // both while the autotuner times kernels of either
-  const bool cpt = p->kernel == 8 || p->kernel == 9 || p->kernel == 10;
+  const bool cpt = p->kernel >= 8 && p->kernel <= 12;
   if (p->precision == PM_PREC_MIXED && !cpt) b += 3 * sizeof(float4) * (size_t)g.alloc4;
   if (p->precision == PM_PREC_MIXED && (cpt || p->kernel < 0))
     b += (3 * sizeof(float4) + sizeof(int4) + sizeof(int2) + sizeof(unsigned)) *
              ((size_t)g.nvox + 1) +
-         sizeof(uint2) * (size_t)compact_words(g);
+         sizeof(uint2) * (size_t)compact_words(g) + sizeof(int2) + 3 * sizeof(unsigned) +
+         sizeof(int);
   b += 8 * (size_t)g.nvox;  // export scratch
   return b + (1 << 20);
 }
@@ -675,6 +685,7 @@ pm_status pm_problem_footprint(const pm_params* p, size_t* bytes) {
 
 pm_status pm_debug_tma_fail(int on) {
   zmarch_debug_fail(on);
+  compact_debug_fail(on);
   return PM_OK;
 }
 
@@ -790,7 +801,7 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       return fail(set_error(PM_ERR_CUDA, "red-black fluid lists do not add up"));
   }
   if (pr->precision == PM_PREC_MIXED) {
-    if (p->kernel == 8 || p->kernel == 9 || p->kernel == 10 || p->kernel < 0) {
+    if ((p->kernel >= 8 && p->kernel <= 12) || p->kernel < 0) {
       const size_t nl = (size_t)pr->nlist + 1;  // and the zero slot
       CKF(dev_alloc((void**)&pr->c_base, 3 * sizeof(float4) * nl));
       CKF(cudaMemsetAsync(pr->c_base, 0, 3 * sizeof(float4) * nl, pr->st));
@@ -798,8 +809,12 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       pr->Ec[1] = pr->c_base + nl;
       pr->Rc = pr->c_base + 2 * nl;
       CKF(dev_alloc((void**)&pr->cslot4, sizeof(int4) * nl));
-      CKF(dev_alloc((void**)&pr->cslot2, sizeof(int2) * nl));
-      CKF(dev_alloc((void**)&pr->cmeta, sizeof(unsigned) * nl));
+      // slots and metadata: three and one entries more than positions, which
+      // the bulk-staged sweep's copies (rounded up to 16 bytes) may read
+      CKF(dev_alloc((void**)&pr->cslot2, sizeof(int2) * (nl + 1)));
+      CKF(dev_alloc((void**)&pr->cmeta, sizeof(unsigned) * (nl + 3)));
+      CKF(dev_alloc((void**)&pr->cerr, sizeof(int)));
+      CKF(cudaMemsetAsync(pr->cerr, 0, sizeof(int), pr->st));
       CKF(dev_alloc((void**)&pr->cwords, sizeof(uint2) * (size_t)compact_words(g)));
     }
     pm_status ts = choose_correction_kernel(pr, p->kernel);
@@ -842,6 +857,7 @@ pm_status pm_problem_destroy(pm_problem* pr) {
   cudaFree(pr->cslot2);
   cudaFree(pr->cmeta);
   cudaFree(pr->cwords);
+  cudaFree(pr->cerr);
   cudaFree(pr->partials);
   cudaFree(pr->dout);
   if (pr->hout) cudaFreeHost(pr->hout);

@@ -26,8 +26,11 @@
 // pm_fast.cu bit for bit: the stencil sees the same numbers (zeros where the
 // padded store holds zeros, images where it holds halo copies) and runs the
 // same update_fast<float>.
+#include <atomic>
+
 #include "pm_compact.h"
 #include "pm_compact.cuh"
+#include "pm_tma.cuh"
 
 namespace pm {
 
@@ -74,6 +77,108 @@ __global__ void __launch_bounds__(256, MINB) k_dc_inner_c(const float4* __restri
     inner_c_compute<SOLVER>(E, E2, R, q, m, sl);
     m = mn;
     sl = sn;
+  }
+}
+
+// Bulk-staged form (kernel 11): the metadata and neighbour slots of a chunk of
+// kChunk consecutive list positions (one per thread) reach shared memory by
+// three untiled bulk copies (cp.async.bulk, one mbarrier per stage counting
+// the bytes), kStages chunks ahead, so each voxel issues its eight correction
+// loads at once instead of after its slot loads; no slot registers are held
+// across voxels.  Thread 0 issues the copies; each warp arrives on the
+// stage's `empty` barrier once its threads have read their entries, and
+// thread 0 waits for all eight before it reuses the stage.  Every wait is
+// bounded (clock64 budget): on expiry the CTA records the failure in *err,
+// thread 0 waits (bounded) for the copies it issued and the CTA returns.
+// The arrays are read past the last position up to the next 16 bytes: meta
+// needs nlist + 4 entries and sb nlist + 2 (compact store allocation).
+// Bitwise equal to kernels 8-10 but slower on the 128^3 sphere pack: 13.4 /
+// 12.4 us per sweep alone at 5 / 4 CTAs per SM against 10.4 us for kernel
+// 10, 3.35 / 3.28 against 2.76 ms per step of the three rotated problems.
+// Each chunk ties the CTA's eight warps to one pipeline (a slow warp holds
+// the refill of its stage), and the 21.5 KB of stages per CTA come out of
+// the L1 that serves the neighbour gathers.  Selectable, not autotuned.
+constexpr int kChunk = 256;
+constexpr int kStages = 3;
+
+template <int SOLVER, int MINB>
+__global__ void __launch_bounds__(kChunk, MINB)
+    k_dc_inner_cb(const float4* __restrict__ E, float4* __restrict__ E2,
+                  const float4* __restrict__ R, const unsigned* __restrict__ meta,
+                  const int4* __restrict__ sa, const int2* __restrict__ sb, int nlist, int* err,
+                  long long budget, int fail_first) {
+  __shared__ __align__(16) int4 s_sa[kStages][kChunk];
+  __shared__ __align__(16) int2 s_sb[kStages][kChunk];
+  __shared__ __align__(16) unsigned s_m[kStages][kChunk];
+  __shared__ __align__(8) unsigned long long full[kStages], empty[kStages];
+  const int nchunks = (nlist + kChunk - 1) / kChunk;
+  const int my = (int)blockIdx.x < nchunks ? (nchunks - 1 - (int)blockIdx.x) / (int)gridDim.x + 1
+                                           : 0;
+  const bool leader = threadIdx.x == 0;
+  if (leader) {
+    for (int s = 0; s < kStages; ++s) {
+      tma::mbar_init(&full[s], 1);
+      tma::mbar_init(&empty[s], kChunk / 32);
+    }
+    tma::fence_mbar_init();
+  }
+  __syncthreads();
+  auto first_pos = [&](int j) {
+    return ((long long)blockIdx.x + (long long)j * gridDim.x) * kChunk;
+  };
+  auto issue = [&](int j) {
+    const int s = j % kStages;
+    const long long q0 = first_pos(j);
+    const int n = (int)min((long long)kChunk, (long long)nlist - q0);
+    const unsigned bm = (unsigned)(n * 4 + 15) & ~15u, bb = (unsigned)(n * 8 + 15) & ~15u,
+                   ba = (unsigned)n * 16u;
+    tma::mbar_expect(&full[s], bm + bb + ba);
+    tma::bulk_g2s(s_m[s], meta + q0, bm, &full[s]);
+    tma::bulk_g2s(s_sb[s], sb + q0, bb, &full[s]);
+    tma::bulk_g2s(s_sa[s], sa + q0, ba, &full[s]);
+  };
+  int issued = 0;
+  if (leader)
+    for (; issued < kStages && issued < my; ++issued) issue(issued);
+  bool ok = true;
+  int j = 0;
+  for (; j < my; ++j) {
+    const int s = j % kStages;
+    const unsigned par = (unsigned)(j / kStages) & 1u;
+    // fail_first (test hook): the first wait reports a timeout without waiting
+    if ((fail_first && j == 0) || !tma::mbar_wait(&full[s], par, budget)) {
+      ok = false;
+      break;
+    }
+    const long long q = first_pos(j) + threadIdx.x;
+    const bool act = q < nlist;
+    unsigned m = 0;
+    CompactSlots sl;
+    if (act) {
+      m = s_m[s][threadIdx.x];
+      sl.a = s_sa[s][threadIdx.x];
+      sl.b = s_sb[s][threadIdx.x];
+    }
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) tma::mbar_arrive(&empty[s]);
+    if (leader && issued < my) {
+      // every warp has read stage s: refill it with chunk j + kStages
+      if (!tma::mbar_wait(&empty[s], par, budget)) {
+        ok = false;
+        break;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(issued);
+      ++issued;
+    }
+    if (act) inner_c_compute<SOLVER>(E, E2, R, (int)q, m, sl);
+  }
+  if (!ok) {
+    atomicExch(err, 1);
+    // drain: thread 0 waits for the copies it issued that nobody waited for
+    if (leader)
+      for (int k = j; k < issued; ++k)
+        tma::mbar_wait(&full[k % kStages], (unsigned)(k / kStages) & 1u, budget);
   }
 }
 
@@ -221,6 +326,39 @@ cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, cons
   if (minb == 3) return inner_c_launch<3, true>(e, e2, r, meta, sa, sb, nlist, solver, st);
   if (minb == 4) return inner_c_launch<4, true>(e, e2, r, meta, sa, sb, nlist, solver, st);
   return inner_c_launch<5, false>(e, e2, r, meta, sa, sb, nlist, solver, st);
+}
+
+// pm_debug_tma_fail: the next bulk-staged sweeps report a timed-out first wait.
+static std::atomic<int> g_cb_fail{0};
+
+void compact_debug_fail(int on) { g_cb_fail.store(on ? 1 : 0); }
+
+template <int MINB>
+static cudaError_t inner_cb_launch(const float4* e, float4* e2, const float4* r,
+                                   const unsigned* meta, const int4* sa, const int2* sb,
+                                   int nlist, int solver, int* err, cudaStream_t st) {
+  const long long budget = 4000000000LL;  // ~2 s at 2 GHz per wait
+  const int ff = g_cb_fail.load();
+  const int blocks = grid_for(nlist, kChunk, MINB * sm_count());
+  if (solver == 1)
+    k_dc_inner_cb<1, MINB><<<blocks, kChunk, 0, st>>>(e, e2, r, meta, sa, sb, nlist, err,
+                                                      budget, ff);
+  else if (solver == 2)
+    k_dc_inner_cb<2, MINB><<<blocks, kChunk, 0, st>>>(e, e2, r, meta, sa, sb, nlist, err,
+                                                      budget, ff);
+  else
+    k_dc_inner_cb<3, MINB><<<blocks, kChunk, 0, st>>>(e, e2, r, meta, sa, sb, nlist, err,
+                                                      budget, ff);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dc_inner_cb(const float4* e, float4* e2, const float4* r,
+                               const unsigned* meta, const int4* sa, const int2* sb, int nlist,
+                               int solver, int minb, int* err, cudaStream_t st) {
+  if (nlist < 1) return cudaSuccess;
+  if (minb >= 5) return inner_cb_launch<5>(e, e2, r, meta, sa, sb, nlist, solver, err, st);
+  return inner_cb_launch<4>(e, e2, r, meta, sa, sb, nlist, solver, err, st);
 }
 
 cudaError_t launch_dc_residual_c(Fields<double> x, float4* r, float4* e, const uint8_t* codes,

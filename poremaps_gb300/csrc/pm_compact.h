@@ -21,6 +21,15 @@ cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, 
 cudaError_t launch_dc_inner_c(const float4* e, float4* e2, const float4* r, const unsigned* meta,
                               const int4* sa, const int2* sb, int nlist, int solver, int minb,
                               cudaStream_t st);
+// The same sweep with each chunk's slots and metadata staged in shared memory
+// by bulk copies (kernels 11 and 12: minb 5 or 4 CTAs per SM).  meta must
+// hold nlist + 4 entries and sb nlist + 2 (the copies round up to 16 bytes).
+// A wait that runs out sets *err (device int) and the launch ends early.
+cudaError_t launch_dc_inner_cb(const float4* e, float4* e2, const float4* r,
+                               const unsigned* meta, const int4* sa, const int2* sb, int nlist,
+                               int solver, int minb, int* err, cudaStream_t st);
+// Test hook: while on, every bulk-staged sweep reports a timed-out first wait.
+void compact_debug_fail(int on);
 // r = F(x) - x (FP64, stored FP32) and e = r.
 cudaError_t launch_dc_residual_c(Fields<double> x, float4* r, float4* e, const uint8_t* codes,
                                  const int* list, int nlist, const Grid& g, int solver,

@@ -49,6 +49,20 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+
+// Untiled bulk copy global -> shared (cp.async.bulk): both addresses 16-byte
+// aligned, bytes a multiple of 16; completes bytes on the barrier's tx count.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_addr(dst)), "l"((unsigned long long)src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void load3(void* dst, const CUtensorMap* map, int x, int y, int z,
                                       unsigned long long* bar) {
   asm volatile(

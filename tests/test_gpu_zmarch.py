@@ -29,7 +29,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
     for kernel, brick in ((1, (0, 0, 0)), (0, (0, 0, 0)), (3, (0, 0, 0)), (2, (32, 8, 8)),
                           (4, (32, 8, 8)), (4, (32, 8, 4)), (4, (32, 4, 4)), (5, (0, 0, 0)),
                           (6, (32, 8, 8)), (7, (0, 0, 0)), (8, (0, 0, 0)), (9, (0, 0, 0)),
-                          (10, (0, 0, 0))):
+                          (10, (0, 0, 0)), (11, (0, 0, 0)), (12, (0, 0, 0))):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=solver, order="jacobi",
                         precision="mixed", kernel=kernel, brick=brick, mixed_inner=40) as p:
             assert p.kernel() == kernel and p.brick() == brick
@@ -43,7 +43,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
 def test_autotuned_kernel_is_a_candidate():
     g = synth.random_solid((32, 32, 32), 0.3, 1)
     with pm.Problem(g, None, solving_algorithm=2, order="jacobi", precision="mixed") as p:
-        assert p.kernel() in tuple(range(11))
+        assert p.kernel() in tuple(range(13))
 
 
 @pytest.mark.parametrize("shape,bc", [((40, 36, 70), 0), ((33, 21, 50), 2)])
@@ -70,7 +70,7 @@ def test_compact_store_small_axes(shape, bc):
     mask word: the compact store equals the padded fluid-list sweep."""
     g = synth.random_solid(shape, 0.25, 3 * sum(shape) + bc)
     out = []
-    for kernel in (1, 8, 9, 10):
+    for kernel in (1, 8, 9, 10, 11, 12):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=2, order="jacobi",
                         precision="mixed", kernel=kernel, mixed_inner=25) as p:
             p.iterate(61)
@@ -86,7 +86,7 @@ def test_compact_store_reductions_mid_block(bc, di):
     open: the compact store's sums equal the padded store's bit for bit."""
     g = synth.random_solid((36, 22, 41), 0.3, 17)
     res = []
-    for kernel in (6, 8, 9, 10):
+    for kernel in (6, 8, 9, 10, 11):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=3, order="jacobi",
                         precision="mixed", kernel=kernel, dom_interest=di) as p:
             p.iterate(157)  # 57 sweeps into a 100-sweep block
@@ -96,11 +96,12 @@ def test_compact_store_reductions_mid_block(bc, di):
     assert all(r == res[0] for r in res[1:])
 
 
-@pytest.mark.parametrize("kernel", [0, 3])
-def test_zmarch_wait_timeout_path(kernel):
-    """The z-march sweep's failure path: with the test hook every CTA treats
-    its first pipeline wait as timed out, sets the error flag and waits for
-    its copies in flight before it returns.  The sweep reports PM_ERR_CUDA;
+@pytest.mark.parametrize("kernel", [0, 3, 11, 12])
+def test_pipeline_wait_timeout_path(kernel):
+    """The failure path of the sweeps fed by asynchronous copies (TMA
+    z-march 0 / 3, bulk-staged compact store 11 / 12): with the test hook
+    every CTA treats its first pipeline wait as timed out, sets the error flag
+    and waits for its copies in flight before it returns.  The sweep reports PM_ERR_CUDA;
     afterwards the same problem, reset, sweeps normally and gives the
     fluid-list kernel's fields bit for bit."""
     g = synth.random_solid((24, 20, 30), 0.3, 41)
