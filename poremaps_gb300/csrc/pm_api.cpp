@@ -266,6 +266,33 @@ void release_unused_store(pm_problem* pr) {
   }
 }
 
+// Tuned correction-sweep choices: (kernel, brick order of the fluid list) per
+// (size, solver, boundary method, porosity bucket).  The choice depends on the
+// medium's size, porosity and boundary family, not on its exact pattern, and
+// every candidate gives bitwise identical fields: problems alike (e.g. the
+// rotated runs of one tensor) share one tuning, and concurrent tunings are
+// serialised instead of timing each other's noise.
+struct Cand {
+  int k, b[3];
+};
+using TuneKey = std::array<long long, 6>;
+std::mutex g_tune_mu;
+std::map<TuneKey, Cand> g_tuned;
+
+TuneKey tune_key(const pm_problem* pr) {
+  return {pr->g.nx, pr->g.ny, pr->g.nz, pr->solver, pr->prm.boundary_method,
+          (long long)llround(20.0 * (double)pr->nlist / (double)pr->g.nvox)};
+}
+
+// The kernel a problem will use if it is already known (pinned, or tuned for
+// a problem alike), else -1: problem creation then allocates only its store.
+int known_kernel(const pm_problem* pr, int kernel) {
+  if (kernel >= 0) return kernel;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto hit = g_tuned.find(tune_key(pr));
+  return hit != g_tuned.end() ? hit->second.k : -1;
+}
+
 pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   const bool tma = zmarch_available() != 0;
   static const int kLex[3] = {0, 0, 0};
@@ -301,21 +328,10 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     if (s != PM_OK) return s;
     return device_sync(pr, "kernel choice");
   }
-  // candidates: (kernel, brick order of the fluid list)
-  struct Cand { int k, b[3]; };
-  // The choice depends on the medium's size, porosity and boundary family,
-  // not on its exact pattern, and every candidate gives bitwise identical
-  // fields: problems alike (e.g. the rotated runs of one tensor) share one
-  // tuning, and concurrent tunings are serialised instead of timing each
-  // other's noise.
-  static std::mutex tune_mu;
-  static std::map<std::array<long long, 6>, Cand> tuned;
-  std::lock_guard<std::mutex> lock(tune_mu);
-  const std::array<long long, 6> key = {
-      pr->g.nx, pr->g.ny, pr->g.nz, pr->solver, pr->prm.boundary_method,
-      (long long)llround(20.0 * (double)pr->nlist / (double)pr->g.nvox)};
-  auto hit = tuned.find(key);
-  if (hit != tuned.end()) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const TuneKey key = tune_key(pr);
+  auto hit = g_tuned.find(key);
+  if (hit != g_tuned.end()) {
     pm_status s = make(hit->second.k, hit->second.b);
     if (s != PM_OK) return s;
     release_unused_store(pr);
@@ -356,7 +372,7 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
   for (int i = 1; i < nc; ++i)
     if (t[i] < t[bi]) bi = i;
   if (t[bi] > 0.95f * t[0]) bi = 0;
-  tuned[key] = cands[bi];
+  g_tuned[key] = cands[bi];
   pm_status s = make(cands[bi].k, cands[bi].b);
   if (s != PM_OK) return s;
   if ((s = zero_corrections(pr)) != PM_OK) return s;
@@ -716,6 +732,16 @@ pm_status pm_params_default(pm_params* p) {
 }
 
 pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem** out) {
+  return problem_create(p, geom, -1, out);
+}
+
+}  // extern "C"
+
+// pm_problem_create; rot_axis 0 / 1: geom is the unrotated volume of the
+// tensor's x / y solve (sizes (nz', nx', ny') / (ny', nz', nx') for the
+// problem's sizes (nx', ny', nz')), rotated on the device after the upload.
+pm_status pm::problem_create(const pm_params* p, const uint8_t* geom, int rot_axis,
+                             pm_problem** out) {
   if (!out) return set_error(PM_ERR_INVALID, "out is NULL");
   *out = nullptr;
   pm_status s = validate(p);
@@ -761,23 +787,23 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
     pr->F[b] = {base + kXoff64, base + g.alloc64 + kXoff64, base + 2 * g.alloc64 + kXoff64,
                 base + 3 * g.alloc64 + kXoff64};
   }
-  if (pr->precision == PM_PREC_MIXED && p->kernel != 8 && p->kernel != 9) {
-    CKF(dev_alloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
-    CKF(cudaMemsetAsync(pr->f32_base, 0, 3 * sizeof(float4) * (size_t)g.alloc4, pr->st));
-    for (int k = 0; k < 3; ++k) {
-      float4* f = pr->f32_base + k * g.alloc4 + kXoff4;
-      if (k < 2) pr->E[k] = f;
-      else pr->R = f;
-    }
-  }
   CKF(dev_alloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
   CKF(dev_alloc((void**)&pr->dout, sizeof(double) * 16));
   CKF(cudaMallocHost((void**)&pr->hout, sizeof(double) * 16));
   pr->scratch_bytes = 8 * (size_t)g.nvox;
   CKF(dev_alloc(&pr->scratch, pr->scratch_bytes));
-  // geometry upload (through the export scratch) -> codes -> fluid list
+  // geometry upload (through the export scratch, 8 bytes per voxel) -> codes
+  // -> fluid list; a rotated solve rotates the upload into the scratch's
+  // second voxel-sized part first
+  const uint8_t* raw = (const uint8_t*)pr->scratch;
   CKF(cudaMemcpyAsync(pr->scratch, geom, (size_t)g.nvox, cudaMemcpyHostToDevice, pr->st));
-  CKF(launch_codes((const uint8_t*)pr->scratch, pr->codes, g, pr->st));
+  if (rot_axis == 0 || rot_axis == 1) {
+    uint8_t* rot = (uint8_t*)pr->scratch + g.nvox;
+    if (rot_axis == 0) CKF(launch_rotate_geom(raw, rot, 0, g.nz, g.nx, g.ny, pr->st));
+    else CKF(launch_rotate_geom(raw, rot, 1, g.ny, g.nz, g.nx, pr->st));
+    raw = rot;
+  }
+  CKF(launch_codes(raw, pr->codes, g, pr->st));
   int* dcount = (int*)pr->dout;
   CKF(launch_fluid_list(pr->codes, g, pr->list, dcount, pr->st));
   unsigned long long* dcnt = (unsigned long long*)((char*)pr->dout + 64);
@@ -801,7 +827,21 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
       return fail(set_error(PM_ERR_CUDA, "red-black fluid lists do not add up"));
   }
   if (pr->precision == PM_PREC_MIXED) {
-    if ((p->kernel >= 8 && p->kernel <= 12) || p->kernel < 0) {
+    // the correction store(s): only the one the kernel uses when it is known
+    // (pinned, or tuned for a problem alike), both while the autotuner times
+    // kernels of either
+    const int kk = known_kernel(pr, p->kernel);
+    const bool want_compact = kk < 0 || (kk >= 8 && kk <= 12);
+    if (kk < 0 || !want_compact) {
+      CKF(dev_alloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
+      CKF(cudaMemsetAsync(pr->f32_base, 0, 3 * sizeof(float4) * (size_t)g.alloc4, pr->st));
+      for (int k = 0; k < 3; ++k) {
+        float4* f = pr->f32_base + k * g.alloc4 + kXoff4;
+        if (k < 2) pr->E[k] = f;
+        else pr->R = f;
+      }
+    }
+    if (want_compact) {
       const size_t nl = (size_t)pr->nlist + 1;  // and the zero slot
       CKF(dev_alloc((void**)&pr->c_base, 3 * sizeof(float4) * nl));
       CKF(cudaMemsetAsync(pr->c_base, 0, 3 * sizeof(float4) * nl, pr->st));
@@ -840,6 +880,8 @@ pm_status pm_problem_create(const pm_params* p, const uint8_t* geom, pm_problem*
   *out = pr;
   return PM_OK;
 }
+
+extern "C" {
 
 pm_status pm_problem_destroy(pm_problem* pr) {
   if (!pr) return PM_OK;

@@ -141,6 +141,9 @@ pm_status cuda_error(cudaError_t e, const char* where);
 pm_status write_log_row(const char* path, bool first, int iteration, double conv, double tps,
                         const pm_result& r);
 size_t problem_device_bytes(const pm_params* p);
+// pm_problem_create; rot_axis 0 / 1 rotates the uploaded geometry on the
+// device for the tensor's x / y solve (launch_rotate_geom), -1 none.
+pm_status problem_create(const pm_params* p, const uint8_t* geom, int rot_axis, pm_problem** out);
 const pm_params* problem_params(const pm_problem* pr);
 long long problem_nvox(const pm_problem* pr);
 cudaStream_t problem_stream(const pm_problem* pr);

@@ -74,6 +74,10 @@ unsigned long long launches_total();
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return the launch error.
 cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cudaStream_t st);
+// The geometry of an axis-rotated tensor solve from the unrotated one (sizes
+// nx, ny, nz of the source): axis 0 -> sizes (ny, nz, nx), axis 1 -> (nz, nx, ny).
+cudaError_t launch_rotate_geom(const uint8_t* src, uint8_t* dst, int axis, int nx, int ny, int nz,
+                               cudaStream_t st);
 // Fluid list in brick order (bx x by x bz bricks; bx <= 0: whole rows,
 // by/bz <= 0: 1, i.e. lexicographic order); parity 0 / 1 keeps only the
 // voxels with (x + y + z) of that parity, < 0 all of them.

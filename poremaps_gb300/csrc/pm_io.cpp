@@ -41,28 +41,6 @@ pm_status write_raw(const std::string& path, const void* data, size_t bytes) {
 
 }  // namespace
 
-namespace {
-
-// Geometry of the run with flow along x (axis 0: z' = x, y' = z, x' = y) or
-// along y (axis 1: z' = y, y' = x, x' = z), README.md:221-225; arrays are
-// x fastest.  Tiled so both the reads and the writes stay in cache.
-void rotate_geometry(const uint8_t* g, int nx, int ny, int nz, int axis, uint8_t* out) {
-  const int T = 16;
-  for (int z0 = 0; z0 < nz; z0 += T)
-    for (int y0 = 0; y0 < ny; y0 += T)
-      for (int x0 = 0; x0 < nx; x0 += T) {
-        const int z1 = std::min(z0 + T, nz), y1 = std::min(y0 + T, ny), x1 = std::min(x0 + T, nx);
-        for (int z = z0; z < z1; ++z)
-          for (int y = y0; y < y1; ++y)
-            for (int x = x0; x < x1; ++x) {
-              const uint8_t v = g[((size_t)z * ny + y) * nx + x];
-              if (axis == 0) out[((size_t)x * nz + z) * ny + y] = v;  // (ny, nz, nx)
-              else out[((size_t)y * nx + x) * nz + z] = v;             // (nz, nx, ny)
-            }
-      }
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -222,19 +200,13 @@ pm_status pm_solve_tensor(const pm_params* p, const uint8_t* geom, double K[9],
   pm_result r[3];
   pm_status st[3] = {PM_OK, PM_OK, PM_OK};
   std::string err[3];
-  // The three solves are independent: each host thread rotates its copy of
-  // the geometry, creates its problem (own stream) and solves it, so the
-  // rotations, set-up and sweeps of the three axes overlap.
+  // The three solves are independent: each host thread creates its problem
+  // (own stream) from the unrotated geometry, which the x and y solves rotate
+  // on the device after the upload, and solves it, so the set-up and sweeps
+  // of the three axes overlap.
   auto run = [&](int a) {
-    std::vector<uint8_t> rot;
-    const uint8_t* g = geom;
-    if (a < 2) {
-      rot.resize((size_t)nx * ny * nz);
-      rotate_geometry(geom, nx, ny, nz, a, rot.data());
-      g = rot.data();
-    }
     pm_problem* pr = nullptr;
-    st[a] = pm_problem_create(&ps[a], g, &pr);
+    st[a] = problem_create(&ps[a], geom, a < 2 ? a : -1, &pr);
     if (st[a] == PM_OK) st[a] = pm_solve(pr, &r[a]);
     if (st[a] != PM_OK) err[a] = pm_last_error();
     pm_problem_destroy(pr);

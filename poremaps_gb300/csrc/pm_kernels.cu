@@ -128,6 +128,40 @@ cudaError_t launch_codes(const uint8_t* raw, uint8_t* codes, const Grid& g, cuda
   return cudaGetLastError();
 }
 
+// Geometry of an axis-rotated solve of the permeability tensor (the flow
+// axis becomes z, as the reference's README.md:221-225 rotates the sample for
+// the x and y runs): src is the x-fastest uint8 volume of sizes (nx, ny, nz);
+// axis 0 writes the volume of sizes (ny, nz, nx) with (x', y', z') =
+// (y, z, x), axis 1 the volume of sizes (nz, nx, ny) with (x', y', z') =
+// (z, x, y).  Coalesced writes, gathered reads.
+__global__ void k_rotate_geom(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                              int axis, int nx, int ny, int nz) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n;
+       o += (long long)gridDim.x * blockDim.x) {
+    long long x, y, z;
+    if (axis == 0) {  // o = (x * nz + z) * ny + y
+      y = o % ny;
+      const long long r = o / ny;
+      z = r % nz;
+      x = r / nz;
+    } else {  // o = (y * nx + x) * nz + z
+      z = o % nz;
+      const long long r = o / nz;
+      x = r % nx;
+      y = r / nx;
+    }
+    dst[o] = src[(z * ny + y) * nx + x];
+  }
+}
+
+cudaError_t launch_rotate_geom(const uint8_t* src, uint8_t* dst, int axis, int nx, int ny, int nz,
+                               cudaStream_t st) {
+  k_rotate_geom<<<1184, 256, 0, st>>>(src, dst, axis, nx, ny, nz);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // Interior fluid voxels as linear interior indices, in brick order: the
 // domain is cut into bricks of BX x BY x BZ voxels (BX = nx, BY = BZ = 1 is
 // plain lexicographic order), bricks are visited lexicographically and the
