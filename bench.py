@@ -169,13 +169,14 @@ def measured_peaks():
         return None
 
 
-def write_case(d, g, max_iter=100000001):
+def write_case(d, g, max_iter=100000001, bc=0, solver=3):
     nz, ny, nx = g.shape
     g.tofile(os.path.join(d, "geom.raw"))
     with open(os.path.join(d, "in.inp"), "w") as f:
-        f.write(f"dom_decomposition 1 1 1\nboundary_method 0\ngeometry_file_name geom.raw\n"
+        f.write(f"dom_decomposition 1 1 1\nboundary_method {bc}\ngeometry_file_name geom.raw\n"
                 f"size_x_y_z  {nx} {ny} {nz}\nvoxel_size  1e-05\nmax_iter    {max_iter}\n"
-                f"it_eval    100\nit_write   100\nlog_file_name run.log\nsolving_algorithm 3\n"
+                f"it_eval    100\nit_write   100\nlog_file_name run.log\n"
+                f"solving_algorithm {solver}\n"
                 f"eps 1e-06\nporosity -1.0\ndom_interest 0 0 0 0 0 0\nwrite_output 0 0 0 0\n")
 
 
@@ -407,7 +408,7 @@ def run_gpu(args):
         if world == 1 and not args.no_serving:
             # the serving target: batched mixed vs plain FP64 solves/h on the
             # uneven stream, and latency percentiles on a request stream
-            out["c4"] = c4_result(args.c4_samples)
+            out["c4"] = c4_result(args.c4_samples, with_cpu=not args.no_cpu_baseline)
             out["c5"] = c5_result(args.c5_requests, args.c5_max_axis)
         print(json.dumps(out), flush=True)
     rep.close()
@@ -716,7 +717,7 @@ def unconverged(results):
     return [i for i, r in enumerate(results) if not r.converged]
 
 
-def c4_result(n_samples: int, relaunch: int = 0):
+def c4_result(n_samples: int, relaunch: int = 0, with_cpu: bool = True):
     """The batched uneven stream (configuration 4) through the mixed-precision
     server against the plain FP64 form solving the samples one by one."""
     import poremaps_gb300 as pm
@@ -747,6 +748,9 @@ def c4_result(n_samples: int, relaunch: int = 0):
             plain.append(p.solve())
     t_64 = time.perf_counter() - t0
     rel, kerr = k_errors([(done[i].result, r) for i, r in enumerate(plain)])
+    cpu = c4_cpu_estimate(reqs, [r.iterations for r in plain]) if with_cpu else None
+    if cpu:
+        cpu["batched_mixed_speedup"] = (3600.0 * len(reqs) / t_mx) / cpu["solves_per_h"]
     unc_mx = unconverged([done[i].result for i in range(len(reqs))])
     unc_64 = unconverged(plain)
     out = {"metric": "solves/h", "value": 3600.0 * len(reqs) / t_mx, "unit": "solves/h",
@@ -765,6 +769,7 @@ def c4_result(n_samples: int, relaunch: int = 0):
                           "unconverged_at_max_iter": unc_64},
            "speedup_vs_plain_fp64": t_64 / t_mx,
            "k_rel_err_vs_plain_fp64": kerr,
+           "cpu_reference_estimate": cpu,
            "iterations": {"min": min(c.result.sweeps for c in done.values()),
                           "max": max(c.result.sweeps for c in done.values())}}
     order = sorted(range(len(rel)), key=lambda i: -rel[i])
@@ -779,6 +784,49 @@ def c4_result(n_samples: int, relaunch: int = 0):
          "fp64": {"iterations": plain[i].iterations, "converged": bool(plain[i].converged),
                   "wk33": plain[i].wk33}} for i in order[:5]]
     return out
+
+
+def c4_cpu_estimate(reqs, iterations, cores=None, sweeps=100):
+    """Solves/h of the reference's CPU path on the c4 stream, as the reference
+    would serve it on this host: one np=1 process per core, each solving one
+    sample.  A subsample of the stream (every k-th sample, one per core) runs
+    `sweeps` reference-order sweeps of the oracle restatement (bitwise the
+    reference program) at once, one process per sample, which gives the
+    per-core MLUP/s under full load; each sample's solve is then
+    voxels x iterations at that rate, with the iterations the plain FP64 GPU
+    form needed for it (Jacobi order; the reference's in-place order needs
+    counts of the same size, e.g. 1,400-1,900 against 1,600-1,900 on the
+    tensor test medium)."""
+    n = len(reqs)
+    cores = cores or min(16, os.cpu_count() or 1)
+    pick = list(range(0, n, max(1, n // cores)))[:cores]
+    cli = oracle_cli()
+    with tempfile.TemporaryDirectory() as root:
+        procs = []
+        for i in pick:
+            d = os.path.join(root, str(i))
+            os.makedirs(d)
+            g, bc = reqs[i]
+            write_case(d, g, bc=bc, solver=SERVE_KW["solving_algorithm"])
+            procs.append((i, subprocess.Popen([cli, "in.inp", "--sweeps", str(sweeps)], cwd=d,
+                                              stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                              text=True)))
+        rates = []
+        for i, pr in procs:
+            out, _ = pr.communicate()
+            if pr.returncode != 0:
+                raise RuntimeError(f"oracle_cli failed on c4 sample {i}")
+            r = json.loads(out.strip().splitlines()[-1])
+            rates.append(reqs[i][0].size * sweeps / r["seconds"])
+    rate = float(np.mean(rates))  # lattice updates per second per core
+    core_s = sum(g.size * it for (g, _), it in zip(reqs, iterations)) / rate
+    sph = 3600.0 * n / (core_s / cores)
+    return {"solves_per_h": sph, "unit": "solves/h", "cores": cores, "kind": "port",
+            "mlups_per_core": rate / 1e6,
+            "sample": f"{len(pick)} of the {n} samples, {sweeps} reference-order sweeps each, "
+                      f"one single-threaded process per sample at once; every sample's solve "
+                      f"extrapolated as voxels x the plain FP64 GPU form's iterations at the "
+                      f"mean per-core rate, {cores} cores"}
 
 
 def run_c4(args):

@@ -63,3 +63,21 @@ def test_fp64_pipe_record(bench_copy):
     f = root / bench.FP64_SOURCES[0]
     f.write_text(f.read_text() + "\n// changed\n")
     assert "stale" in bench.fp64_pipe_record(10, 0.1)
+
+
+def test_c4_cpu_estimate_extrapolates_measured_rates():
+    """The c4 leg's CPU figure: the oracle restatement's reference-order
+    sweeps on a subsample, one process per sample, extrapolated to the whole
+    stream by voxels x iterations at the measured per-core rate."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    from poremaps_gb300 import synth
+    reqs = [(synth.random_solid((10, 12, 14), 0.3, s), s % 2) for s in range(4)]
+    iters = [1000, 2000, 1500, 3000]
+    est = bench.c4_cpu_estimate(reqs, iters, cores=2, sweeps=20)
+    assert est["cores"] == 2 and est["kind"] == "port" and est["mlups_per_core"] > 0
+    rate = est["mlups_per_core"] * 1e6
+    core_s = sum(g.size * it for (g, _), it in zip(reqs, iters)) / rate
+    assert np.isclose(est["solves_per_h"], 3600.0 * len(reqs) / (core_s / 2))
+    assert "2 of the 4 samples" in est["sample"]

@@ -62,3 +62,26 @@ def test_tensor_matches_reference_program(solver, precision):
     assert np.abs(K - K_log).max() <= 1e-6 * scale  # the reference log's 7 digits
     print(f"solver {solver} {precision}: reference iterations {its}, "
           f"GPU iterations {[r.iterations for r in res]}")
+
+
+@pytest.mark.parametrize("precision,bc", [("fp64", 0), ("mixed", 1), ("fp64", 3)])
+def test_tensor_rotations_on_a_non_cubic_medium(precision, bc):
+    """pm_solve_tensor rotates the geometry of the x and y solves on the
+    device.  On a medium with three different axis lengths (where a mix-up of
+    the rotated sizes shows), every component equals three problems created
+    from geometry rotated on the host, bit for bit: flow along x sees sizes
+    (ny, nz, nx) with (x', y', z') = (y, z, x), flow along y (nz, nx, ny) with
+    (x', y', z') = (z, x, y) (README.md:221-225 of the reference)."""
+    from poremaps_gb300 import synth
+    g = synth.random_solid((14, 11, 9), 0.3, 23)  # (nz, ny, nx)
+    kw = dict(boundary_method=bc, solving_algorithm=2, voxel_size=1e-5, eps=1e-30,
+              max_iter=1300, precision=precision)
+    K, res = pm.solve_tensor(g, None, **kw)
+    rot = {"x": np.transpose(g, (2, 0, 1)), "y": np.transpose(g, (1, 2, 0)), "z": g}
+    want = np.zeros((3, 3))
+    for axis in "xyz":
+        with pm.Problem(np.ascontiguousarray(rot[axis]), None, **kw) as p:
+            r = p.solve()
+        for (i, j), v in zip(SLOTS[axis], (r.wk13, r.wk23, r.wk33)):
+            want[i, j] = v
+    assert np.array_equal(K, want), np.abs(K - want).max()
