@@ -737,6 +737,7 @@ def c4_result(n_samples: int, relaunch: int = 0, with_cpu: bool = True):
             done[tickets[c.ticket]] = c
     t_mx = time.perf_counter() - t0
     busy, wall, lups = srv.stats()
+    shape = srv.launch_shape()  # the autotuner's choice for the last resident set
     srv.close()
     # plain FP64 GPU form, one sample after another (Jacobi order, FMA form: the
     # fastest FP64 form and the same ordering as the mixed form)
@@ -763,7 +764,8 @@ def c4_result(n_samples: int, relaunch: int = 0, with_cpu: bool = True):
                              "converged_solves_per_h":
                                  3600.0 * (len(reqs) - len(unc_mx)) / t_mx,
                              "unconverged_at_max_iter": unc_mx,
-                             "device_busy_ms": busy, "glups_busy": lups / (busy * 1e6)},
+                             "device_busy_ms": busy, "glups_busy": lups / (busy * 1e6),
+                             "launch_shape_last": shape},
            "plain_fp64": {"solves_per_h": 3600.0 * len(reqs) / t_64, "seconds": t_64,
                           "converged_solves_per_h": 3600.0 * (len(reqs) - len(unc_64)) / t_64,
                           "unconverged_at_max_iter": unc_64},

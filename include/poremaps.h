@@ -273,7 +273,8 @@ typedef struct {
   int max_resident;         /* slot limit (0 = 1024) */
   int precision;            /* pm_precision for all requests */
   int use_graphs;           /* capture each it_eval block of sweeps in a CUDA graph */
-  int autotune;             /* pick tile shapes per size class by timing */
+  int autotune;             /* pick the launch shape (pm_server_launch_shape) per size
+                               class of the resident set by timing */
   int max_bypass;           /* backfill: when the request at the head of the queue does
                                not fit the free budget, later requests that fit are
                                admitted past it, at most max_bypass times before the
@@ -316,6 +317,17 @@ pm_status pm_server_cancel(pm_server* s, uint64_t ticket);
  * server's precision and kernels), to plan budgets.  No counterpart in the
  * reference. */
 pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* bytes);
+/* Launch shape of the batched sweeps: shape[0] voxels per work item (the tile
+ * of the device queue; cut smaller when the resident set is small), shape[1]
+ * CTAs per SM and shape[2] threads per block of the mixed form's persistent
+ * round, shape[3] threads per block of the other batched kernels.  With
+ * cfg.autotune the server picks them per size class of the resident set; the
+ * getter reports the current choice.  The setter pins a shape (autotuning
+ * stops; 128 threads with 1-8 CTAs or 256 with 1-4, threads 128 / 256 / 512)
+ * from the next round on; call it between rounds.  Every shape gives the same
+ * results bit for bit.  No counterpart in the reference. */
+pm_status pm_server_launch_shape(pm_server* s, int shape[4]);
+pm_status pm_server_set_launch_shape(pm_server* s, const int shape[4]);
 
 /* ---- test hook (no counterpart in the reference) ----
  * Makes the nth device allocation of problem set-up from now on (1 = the next

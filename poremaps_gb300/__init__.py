@@ -91,7 +91,7 @@ EXPORTS = ["pm_last_error", "pm_last_error_copy", "pm_version", "pm_params_defau
            "pm_server_submit", "pm_server_step", "pm_server_poll", "pm_server_stats",
            "pm_server_clock_ms", "pm_server_cancel", "pm_debug_fail_alloc",
            "pm_problem_footprint", "pm_server_request_bytes", "pm_debug_round_wait",
-           "pm_debug_tma_fail"]
+           "pm_debug_tma_fail", "pm_server_launch_shape", "pm_server_set_launch_shape"]
 
 _lib = None
 
@@ -154,6 +154,8 @@ def load_library(path: str = LIB_PATH):
         "pm_debug_tma_fail": (C.c_int, [C.c_int]),
         "pm_problem_footprint": (C.c_int, [P(Params), P(C.c_size_t)]),
         "pm_server_request_bytes": (C.c_int, [vp, P(Params), P(C.c_size_t)]),
+        "pm_server_launch_shape": (C.c_int, [vp, P(C.c_int)]),
+        "pm_server_set_launch_shape": (C.c_int, [vp, P(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):
@@ -430,6 +432,19 @@ class Server:
 
     def clock_ms(self) -> float:
         return load_library().pm_server_clock_ms(self.h)
+
+    def launch_shape(self) -> dict:
+        """pm_server_launch_shape: the batched sweeps' current launch shape."""
+        v = (C.c_int * 4)()
+        _check(load_library().pm_server_launch_shape(self.h, v))
+        return {"item_voxels": v[0], "round_ctas_per_sm": v[1], "round_threads": v[2],
+                "threads": v[3]}
+
+    def set_launch_shape(self, item_voxels: int, round_ctas_per_sm: int, round_threads: int,
+                         threads: int) -> None:
+        """pm_server_set_launch_shape: pin the launch shape (no autotuning)."""
+        v = (C.c_int * 4)(item_voxels, round_ctas_per_sm, round_threads, threads)
+        _check(load_library().pm_server_set_launch_shape(self.h, v))
 
     def request_bytes(self, geom: np.ndarray, **kw) -> int:
         """pm_server_request_bytes: the footprint this server admits the

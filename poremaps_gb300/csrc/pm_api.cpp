@@ -62,6 +62,46 @@ cudaError_t dev_alloc(T** ptr, size_t bytes) {
   return cudaMalloc((void**)ptr, bytes);
 }
 
+// Sub-buffers of one device allocation, each on a 256-byte boundary (the
+// alignment cudaMalloc gives): a problem's fixed buffers and its compact
+// store are one allocation each, so that concurrent set-ups (the tensor's
+// three rotations, the server's admissions) make a few driver calls each
+// instead of one per buffer.
+struct Carve {
+  size_t bytes = 0;
+  size_t take(size_t n) {
+    const size_t o = bytes;
+    bytes = (bytes + n + 255) & ~(size_t)255;
+    return o;
+  }
+};
+
+// Pinned host result buffers (256 bytes per problem) from a process-wide pool
+// of 64 KB slabs that lives until exit: cudaMallocHost is a slow driver call
+// and cudaFreeHost waits for the device.  A buffer goes back to the pool only
+// after its problem's stream is synchronised.
+std::mutex g_pin_mu;
+std::vector<double*> g_pin_free;
+
+cudaError_t pinned_slot(double** out) {
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  if (g_pin_free.empty()) {
+    void* slab = nullptr;
+    cudaError_t e = cudaMallocHost(&slab, 65536);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < 65536 / 256; ++i) g_pin_free.push_back((double*)((char*)slab + 256 * i));
+  }
+  *out = g_pin_free.back();
+  g_pin_free.pop_back();
+  return cudaSuccess;
+}
+
+void pinned_release(double* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(p);
+}
+
 pm_status cuda_error(cudaError_t e, const char* where) {
   if (e == cudaErrorMemoryAllocation)
     return set_error(PM_ERR_NOMEM, "%s: %s", where, cudaGetErrorString(e));
@@ -251,12 +291,8 @@ void release_unused_store(pm_problem* pr) {
     pr->f32_base = nullptr;
     pr->E[0] = pr->E[1] = pr->R = nullptr;
   } else {
-    cudaFree(pr->c_base);
-    cudaFree(pr->cslot4);
-    cudaFree(pr->cslot2);
-    cudaFree(pr->cmeta);
-    cudaFree(pr->cwords);
-    cudaFree(pr->cerr);
+    cudaFree(pr->carena);
+    pr->carena = nullptr;
     pr->cerr = nullptr;
     pr->c_base = pr->Ec[0] = pr->Ec[1] = pr->Rc = nullptr;
     pr->cslot4 = nullptr;
@@ -777,21 +813,35 @@ pm_status pm::problem_create(const pm_params* p, const uint8_t* geom, int rot_ax
   sm_count();  // device query outside any later graph capture
   CKF(cudaEventCreate(&pr->ev0));
   CKF(cudaEventCreate(&pr->ev1));
-  CKF(dev_alloc((void**)&pr->codes_base, g.allocc));
+  // the fixed buffers: codes, fluid list, the two FP64 states, reduction
+  // partials and results, export scratch (one allocation)
+  pr->scratch_bytes = 8 * (size_t)g.nvox;
+  {
+    Carve c;
+    const size_t o_codes = c.take(g.allocc);
+    const size_t o_list = c.take(sizeof(int) * (size_t)(g.nvox > 0 ? g.nvox : 1));
+    const size_t o_f64[2] = {c.take(4 * sizeof(double) * (size_t)g.alloc64),
+                             c.take(4 * sizeof(double) * (size_t)g.alloc64)};
+    const size_t o_part = c.take(sizeof(double) * kRedBlocks * kRedVals + 64);
+    const size_t o_dout = c.take(sizeof(double) * 16);
+    const size_t o_scr = c.take(pr->scratch_bytes);
+    CKF(dev_alloc((void**)&pr->arena, c.bytes));
+    char* a = (char*)pr->arena;
+    pr->codes_base = (uint8_t*)(a + o_codes);
+    pr->list = (int*)(a + o_list);
+    for (int b = 0; b < 2; ++b) pr->f64_base[b] = (double*)(a + o_f64[b]);
+    pr->partials = (double*)(a + o_part);
+    pr->dout = (double*)(a + o_dout);
+    pr->scratch = a + o_scr;
+  }
   pr->codes = pr->codes_base + kXoffC;
   CKF(cudaMemsetAsync(pr->codes_base, 0, g.allocc, pr->st));
-  CKF(dev_alloc((void**)&pr->list, sizeof(int) * (size_t)(g.nvox > 0 ? g.nvox : 1)));
   for (int b = 0; b < 2; ++b) {
-    CKF(dev_alloc((void**)&pr->f64_base[b], 4 * sizeof(double) * (size_t)g.alloc64));
     double* base = pr->f64_base[b];
     pr->F[b] = {base + kXoff64, base + g.alloc64 + kXoff64, base + 2 * g.alloc64 + kXoff64,
                 base + 3 * g.alloc64 + kXoff64};
   }
-  CKF(dev_alloc((void**)&pr->partials, sizeof(double) * kRedBlocks * kRedVals + 64));
-  CKF(dev_alloc((void**)&pr->dout, sizeof(double) * 16));
-  CKF(cudaMallocHost((void**)&pr->hout, sizeof(double) * 16));
-  pr->scratch_bytes = 8 * (size_t)g.nvox;
-  CKF(dev_alloc(&pr->scratch, pr->scratch_bytes));
+  CKF(pinned_slot(&pr->hout));
   // geometry upload (through the export scratch, 8 bytes per voxel) -> codes
   // -> fluid list; a rotated solve rotates the upload into the scratch's
   // second voxel-sized part first
@@ -842,20 +892,30 @@ pm_status pm::problem_create(const pm_params* p, const uint8_t* geom, int rot_ax
       }
     }
     if (want_compact) {
+      // e0, e1, r, slots, metadata, error flag, mask words (one allocation);
+      // slots and metadata hold one and three entries more than positions,
+      // which the bulk-staged sweep's copies (rounded up to 16 bytes) may read
       const size_t nl = (size_t)pr->nlist + 1;  // and the zero slot
-      CKF(dev_alloc((void**)&pr->c_base, 3 * sizeof(float4) * nl));
+      Carve c;
+      const size_t o_e = c.take(3 * sizeof(float4) * nl);
+      const size_t o_s4 = c.take(sizeof(int4) * nl);
+      const size_t o_s2 = c.take(sizeof(int2) * (nl + 1));
+      const size_t o_m = c.take(sizeof(unsigned) * (nl + 3));
+      const size_t o_err = c.take(sizeof(int));
+      const size_t o_w = c.take(sizeof(uint2) * (size_t)compact_words(g));
+      CKF(dev_alloc((void**)&pr->carena, c.bytes));
+      char* a = (char*)pr->carena;
+      pr->c_base = (float4*)(a + o_e);
+      pr->cslot4 = (int4*)(a + o_s4);
+      pr->cslot2 = (int2*)(a + o_s2);
+      pr->cmeta = (unsigned*)(a + o_m);
+      pr->cerr = (int*)(a + o_err);
+      pr->cwords = (uint2*)(a + o_w);
       CKF(cudaMemsetAsync(pr->c_base, 0, 3 * sizeof(float4) * nl, pr->st));
+      CKF(cudaMemsetAsync(pr->cerr, 0, sizeof(int), pr->st));
       pr->Ec[0] = pr->c_base;
       pr->Ec[1] = pr->c_base + nl;
       pr->Rc = pr->c_base + 2 * nl;
-      CKF(dev_alloc((void**)&pr->cslot4, sizeof(int4) * nl));
-      // slots and metadata: three and one entries more than positions, which
-      // the bulk-staged sweep's copies (rounded up to 16 bytes) may read
-      CKF(dev_alloc((void**)&pr->cslot2, sizeof(int2) * (nl + 1)));
-      CKF(dev_alloc((void**)&pr->cmeta, sizeof(unsigned) * (nl + 3)));
-      CKF(dev_alloc((void**)&pr->cerr, sizeof(int)));
-      CKF(cudaMemsetAsync(pr->cerr, 0, sizeof(int), pr->st));
-      CKF(dev_alloc((void**)&pr->cwords, sizeof(uint2) * (size_t)compact_words(g)));
     }
     pm_status ts = choose_correction_kernel(pr, p->kernel);
     if (ts != PM_OK) return fail(ts);
@@ -889,21 +949,10 @@ pm_status pm_problem_destroy(pm_problem* pr) {
   for (auto& b : pr->graphs) cudaGraphExecDestroy(b.exec);
   zmarch_destroy(pr->zp);
   brick_destroy(pr->bp);
-  cudaFree(pr->codes_base);
-  cudaFree(pr->list);
-  cudaFree(pr->f64_base[0]);
-  cudaFree(pr->f64_base[1]);
+  cudaFree(pr->arena);
   cudaFree(pr->f32_base);
-  cudaFree(pr->c_base);
-  cudaFree(pr->cslot4);
-  cudaFree(pr->cslot2);
-  cudaFree(pr->cmeta);
-  cudaFree(pr->cwords);
-  cudaFree(pr->cerr);
-  cudaFree(pr->partials);
-  cudaFree(pr->dout);
-  if (pr->hout) cudaFreeHost(pr->hout);
-  cudaFree(pr->scratch);
+  cudaFree(pr->carena);
+  pinned_release(pr->hout);
   if (pr->ev0) cudaEventDestroy(pr->ev0);
   if (pr->ev1) cudaEventDestroy(pr->ev1);
   if (pr->st) cudaStreamDestroy(pr->st);

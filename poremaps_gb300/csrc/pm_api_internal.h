@@ -71,7 +71,10 @@ struct pm_problem {
   int precision = PM_PREC_FP64;
   int solver = 2;
   int exact = 1;
-  // device memory
+  // device memory: `arena` holds codes, list, both FP64 states, partials,
+  // dout and scratch; `carena` the compact store; f32_base the padded store
+  void* arena = nullptr;
+  void* carena = nullptr;
   uint8_t* codes_base = nullptr;
   uint8_t* codes = nullptr;
   int* list = nullptr;
@@ -97,7 +100,7 @@ struct pm_problem {
   int* cerr = nullptr;  // bulk-staged compact sweep (kernels 11, 12): a wait ran out
   double* partials = nullptr;
   double* dout = nullptr;
-  double* hout = nullptr;  // pinned
+  double* hout = nullptr;  // pinned (a 256-byte slot of the process-wide pool)
   void* scratch = nullptr;  // export buffer
   size_t scratch_bytes = 0;
   int coop_blocks = 0;

@@ -209,10 +209,13 @@ void launch_solver_kind(int kind, int grid, int threads, const SampleDesc* d,
 
 cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
                                int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
-                               int solver, unsigned extra, int polls, int ctas_per_sm) {
+                               int solver, unsigned extra, int polls, int ctas_per_sm,
+                               int threads) {
   if (polls <= 0) polls = kMaxPolls;
+  threads = threads == 128 ? 128 : 256;  // the kernel's 64 registers: 8 / 4 CTAs per SM
+  const int max_ctas = threads == 128 ? 8 : 4;
   if (ctas_per_sm < 1) ctas_per_sm = 1;
-  if (ctas_per_sm > 4) ctas_per_sm = 4;
+  if (ctas_per_sm > max_ctas) ctas_per_sm = max_ctas;
   cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(unsigned) * (2 + (size_t)nsamples), st);
   if (e != cudaSuccess) return e;
   if (nitems <= 0 || sweeps <= 0) return cudaSuccess;
@@ -220,13 +223,13 @@ cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int n
   int grid = ctas_per_sm * sm_count();
   if (tickets < grid) grid = (int)tickets;
   if (solver == 1)
-    k_batch_inner_round<1><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+    k_batch_inner_round<1><<<grid, threads, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
   else if (solver == 2)
-    k_batch_inner_round<2><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+    k_batch_inner_round<2><<<grid, threads, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
   else if (solver == 3)
-    k_batch_inner_round<3><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+    k_batch_inner_round<3><<<grid, threads, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
   else
-    k_batch_inner_round<0><<<grid, 256, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
+    k_batch_inner_round<0><<<grid, threads, 0, st>>>(d, items, nitems, sweeps, sync, extra, polls);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -48,11 +48,12 @@ cudaError_t launch_batch(int kind, const SampleDesc* d, const WorkItem* items, i
 // (launch_batch_round clears them itself).  extra / polls: the test hook of
 // pm_debug_round_wait (a target that is never reached, a short poll limit);
 // 0 / 0 in normal operation.
-// ctas_per_sm: resident CTAs of 256 threads per SM the persistent grid holds
-// (1..4; the server's autotuner picks it).
+// ctas_per_sm / threads: resident CTAs per SM the persistent grid holds and
+// their block size (128: 1..8 CTAs, 256: 1..4; the server's autotuner picks
+// both).
 cudaError_t launch_batch_round(const SampleDesc* d, const WorkItem* items, int nitems,
                                int nsamples, int sweeps, unsigned* sync, cudaStream_t st,
                                int solver = 0, unsigned extra = 0, int polls = 0,
-                               int ctas_per_sm = 4);
+                               int ctas_per_sm = 4, int threads = 256);
 
 }  // namespace pm

@@ -90,7 +90,9 @@ struct pm_server {
   cudaGraphExec_t gexec = nullptr;
   int graph_kernels = 0;
   int threads = 256, chunk = 8192;
-  int round_ctas = 4;  // CTAs per SM of the persistent round kernel
+  int round_ctas = 4;      // CTAs per SM of the persistent round kernel
+  int round_threads = 256;  // and their block size
+  bool shape_pinned = false;  // pm_server_set_launch_shape: no autotuning
   int solver = 0;  // the solver every resident sample uses, 0 when they differ
   long long tuned_for = -1;
   double busy_ms = 0.0;
@@ -318,7 +320,7 @@ pm_status issue_block(pm_server* s, int* nk) {
     } else if (s->block > 1) {
       SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), s->block - 1,
                              s->d_sync, s->st, s->solver, g_round_extra.load(),
-                             g_round_polls.load(), s->round_ctas));
+                             g_round_polls.load(), s->round_ctas, s->round_threads));
       ++k;
     }
     SCK(launch_batch(kBatchCorrect, s->d_desc, s->d_items, n, s->block, T, 0, nullptr, s->st));
@@ -337,8 +339,9 @@ pm_status issue_block(pm_server* s, int* nk) {
 
 // Launch shape of the batched sweeps, timed on the current resident set:
 // the work-item size (voxels per tile of the queue) and, for the persistent
-// round, the CTAs per SM of its grid (a 3-sweep round per candidate); for
-// one launch per sweep, the threads per block.  Decisions are kept per size
+// round, the block size and CTAs per SM of its grid (128 or 256 threads at
+// the same range of resident warps; a 3-sweep round per candidate); for one
+// launch per sweep, the threads per block.  Decisions are kept per size
 // class (precision, launch form, solver, log2 of the resident fluid voxels,
 // log2 of the resident samples), so a stream whose resident set keeps its
 // size tunes once.  Safe at a block boundary: the timed launches only write
@@ -351,7 +354,7 @@ struct TuneKey {
   }
 };
 struct TuneVal {
-  int threads, chunk, ctas;
+  int threads, chunk, ctas, round_threads;
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneVal> g_tuned;
@@ -366,6 +369,7 @@ pm_status autotune(pm_server* s) {
   static const int kThreads[] = {128, 256, 512};
   static const int kChunks[] = {2048, 8192, 32768};
   static const int kCtas[] = {2, 3, 4};
+  static const int kRoundThreads[] = {256, 128};
   long long total = 0;
   for (auto& r : s->res) total += r.pr->nlist;
   if (s->tuned_for > 0 && total < 4 * s->tuned_for && 4 * total > s->tuned_for) return PM_OK;
@@ -379,12 +383,13 @@ pm_status autotune(pm_server* s) {
       s->threads = it->second.threads;
       s->chunk = it->second.chunk;
       s->round_ctas = it->second.ctas;
+      s->round_threads = it->second.round_threads;
       s->tuned_for = total;
       return PM_OK;
     }
   }
   float best = 1e30f;
-  int bt = s->threads, bc = s->chunk, bm = s->round_ctas;
+  int bt = s->threads, bc = s->chunk, bm = s->round_ctas, brt = s->round_threads;
   const int kind = mixed(s) ? kBatchInner : kBatchSweep64;
   auto time_it = [&](auto&& issue, float* ms) -> pm_status {
     pm_status e = issue();  // warm-up
@@ -397,22 +402,24 @@ pm_status autotune(pm_server* s) {
     SCK(cudaEventElapsedTime(ms, s->e0, s->e1));
     return PM_OK;
   };
+  // persistent round: the work-item size at the current block shape first,
+  // then the block shape for that size (9 timed rounds, not 3 x 6)
+  auto time_round = [&](int n, int m, int rt, float* ms) -> pm_status {
+    return time_it([&]() -> pm_status {
+      SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), 3, s->d_sync,
+                             s->st, s->solver, 0, 0, m, rt));
+      return PM_OK;
+    }, ms);
+  };
   for (int c : kChunks) {
     build_items(s, c);
     pm_status e = upload(s);
     if (e != PM_OK) return e;
     const int n = (int)s->h_items.size();
     if (persistent) {
-      for (int m : kCtas) {
-        float ms = 0.f;
-        e = time_it([&]() -> pm_status {
-          SCK(launch_batch_round(s->d_desc, s->d_items, n, (int)s->h_desc.size(), 3, s->d_sync,
-                                 s->st, s->solver, 0, 0, m));
-          return PM_OK;
-        }, &ms);
-        if (e != PM_OK) return e;
-        if (ms < best) { best = ms; bc = c; bm = m; }
-      }
+      float ms = 0.f;
+      if ((e = time_round(n, bm, brt, &ms)) != PM_OK) return e;
+      if (ms < best) { best = ms; bc = c; }
     } else {
       for (int t : kThreads) {
         float ms = 0.f;
@@ -425,12 +432,33 @@ pm_status autotune(pm_server* s) {
       }
     }
   }
+  if (persistent) {
+    build_items(s, bc);
+    pm_status e = upload(s);
+    if (e != PM_OK) return e;
+    const int n = (int)s->h_items.size();
+    const int m_in = bm, rt_in = brt;
+    // another block shape only for a clear win: a 3-sweep round is short,
+    // and 128-thread rounds that won such trials by a few per cent were
+    // slower over whole runs (c4: 117-118 k against 121-122 k solves/h)
+    const float keep = 0.95f * best;
+    float best2 = keep;
+    for (int rt : kRoundThreads)
+      for (int m0 : kCtas) {
+        const int m = m0 * (256 / rt);  // the same resident warps at either block size
+        if (m == m_in && rt == rt_in) continue;  // timed in the first stage
+        float ms = 0.f;
+        if ((e = time_round(n, m, rt, &ms)) != PM_OK) return e;
+        if (ms < best2) { best2 = ms; bm = m; brt = rt; }
+      }
+  }
   s->threads = bt;
   s->chunk = bc;
   s->round_ctas = bm;
+  s->round_threads = brt;
   s->tuned_for = total;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tuned[key] = {bt, bc, bm};
+  g_tuned[key] = {bt, bc, bm, brt};
   return PM_OK;
 }
 
@@ -466,7 +494,7 @@ pm_status rebuild(pm_server* s) {
     s->h_desc.push_back(d);
   }
   pm_status e;
-  if (s->cfg.autotune && (e = autotune(s)) != PM_OK) return e;
+  if (s->cfg.autotune && !s->shape_pinned && (e = autotune(s)) != PM_OK) return e;
   build_items(s, s->chunk);
   if ((e = upload(s)) != PM_OK) return e;
   drop_graph(s);
@@ -675,6 +703,34 @@ pm_status pm_server_request_bytes(pm_server* s, const pm_params* p, size_t* byte
   q.prm = *p;
   pm_params rp = request_params(s, q);
   return pm_problem_footprint(&rp, bytes);
+}
+
+pm_status pm_server_launch_shape(pm_server* s, int shape[4]) {
+  if (!s || !shape) return set_error(PM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  shape[0] = s->chunk;
+  shape[1] = s->round_ctas;
+  shape[2] = s->round_threads;
+  shape[3] = s->threads;
+  return PM_OK;
+}
+
+pm_status pm_server_set_launch_shape(pm_server* s, const int shape[4]) {
+  if (!s || !shape) return set_error(PM_ERR_INVALID, "bad arguments");
+  const int chunk = shape[0], ctas = shape[1], rt = shape[2], t = shape[3];
+  if (chunk < 1 || (rt != 128 && rt != 256) || ctas < 1 || ctas > (rt == 128 ? 8 : 4) ||
+      (t != 128 && t != 256 && t != 512))
+    return set_error(PM_ERR_INVALID,
+                     "launch shape: voxels per item >= 1, round threads 128 (1-8 CTAs per SM) "
+                     "or 256 (1-4), threads 128, 256 or 512");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->chunk = chunk;
+  s->round_ctas = ctas;
+  s->round_threads = rt;
+  s->threads = t;
+  s->shape_pinned = true;
+  s->dirty = true;  // items and graph are rebuilt at the next round
+  return PM_OK;
 }
 
 pm_status pm_server_cancel(pm_server* s, uint64_t ticket) {

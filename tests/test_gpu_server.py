@@ -32,10 +32,12 @@ def samples(n=6, seed=0):
 
 
 def run_server(geoms, precision="mixed", use_graphs=1, autotune=0, budget=0, kw=None,
-               submit_later=(), relaunch_sweeps=0):
+               submit_later=(), relaunch_sweeps=0, shape=None, shapes_seen=None):
     kw = dict(KW, **(kw or {}))
     s = pm.Server(precision=precision, use_graphs=use_graphs, autotune=autotune,
                   hbm_budget_bytes=budget, relaunch_sweeps=relaunch_sweeps)
+    if shape is not None:
+        s.set_launch_shape(*shape)
     tickets = {}
     for i, g in enumerate(geoms):
         if i not in submit_later:
@@ -52,6 +54,8 @@ def run_server(geoms, precision="mixed", use_graphs=1, autotune=0, budget=0, kw=
             active = 1
         for c in s.poll():
             results[tickets[c.ticket]] = c
+        if shapes_seen is not None:
+            shapes_seen.append(s.launch_shape())
         if active == 0 and len(results) == len(geoms):
             break
         assert steps < 5000
@@ -314,7 +318,9 @@ def test_allocation_failure_is_reported_and_recovered():
     PM_ERR_NOMEM from pm_problem_create and in the server's completion;
     nothing leaks and the next requests run normally."""
     g = samples(2, seed=8)
-    for nth in (1, 3, 6):
+    # a mixed problem makes two or three device allocations: its fixed
+    # buffers, then the correction store(s)
+    for nth in (1, 2):
         pm.debug_fail_alloc(nth)
         with pytest.raises(RuntimeError, match="PM_ERR_NOMEM"):
             pm.Problem(g[0], None, precision="mixed", order="jacobi", **KW)
@@ -367,3 +373,37 @@ def test_round_wait_that_runs_out_reports_an_error():
     res = run_server(geoms)
     for i, g in enumerate(geoms):
         assert res[i].status == 0 and res[i].result.wk33 == single(g).wk33
+
+
+def test_launch_shapes_give_identical_results():
+    """The persistent round at 256 threads x 4 CTAs per SM and at 128 threads
+    x 8, with different work-item sizes and block sizes of the other batched
+    kernels, and the autotuned shape: the same results bit for bit.  Every
+    shape the autotuner picks is one of its candidates."""
+    geoms = samples(5, seed=7)
+    outs = []
+    for shape in ((8192, 4, 256, 256), (512, 8, 128, 128), (2048, 3, 128, 512)):
+        seen = []
+        outs.append(run_server(geoms, shape=shape, shapes_seen=seen))
+        assert all(tuple(d.values()) == shape for d in seen)
+    seen = []
+    outs.append(run_server(geoms, autotune=1, shapes_seen=seen))
+    for d in seen:
+        assert d["item_voxels"] in (2048, 8192, 32768) and d["threads"] == 256
+        assert (d["round_threads"], d["round_ctas_per_sm"]) in (
+            (256, 2), (256, 3), (256, 4), (128, 4), (128, 6), (128, 8))
+    for other in outs[1:]:
+        for i in range(len(geoms)):
+            a, b = outs[0][i].result, other[i].result
+            assert a.iterations == b.iterations
+            for f in ("wk13", "wk23", "wk33", "wmax_velz", "wmean_velz"):
+                assert getattr(a, f) == getattr(b, f), (i, f)
+
+
+def test_launch_shape_rejects_invalid_shapes():
+    s = pm.Server(precision="mixed")
+    for bad in ((0, 4, 256, 256), (8192, 5, 256, 256), (8192, 9, 128, 256),
+                (8192, 4, 192, 256), (8192, 4, 256, 96)):
+        with pytest.raises(pm.PMError):
+            s.set_launch_shape(*bad)
+    s.close()
