@@ -293,6 +293,7 @@ void release_unused_store(pm_problem* pr) {
   } else {
     cudaFree(pr->carena);
     pr->carena = nullptr;
+    pr->compact_ready = false;
     pr->cerr = nullptr;
     pr->c_base = pr->Ec[0] = pr->Ec[1] = pr->Rc = nullptr;
     pr->cslot4 = nullptr;
@@ -340,14 +341,19 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     pr->kern = k;
     const bool cpt = k >= 8 && k <= 12;
     if (cpt) b = kLex;
-    {
+    // the list is rebuilt only when its order changes (creation builds it
+    // lexicographic), and the compact store is set up once per list order
+    if (b[0] != pr->brick[0] || b[1] != pr->brick[1] || b[2] != pr->brick[2]) {
       int* dcount = (int*)pr->dout;
       CK(launch_fluid_list(pr->codes, pr->g, pr->list, dcount, pr->st, b[0], b[1], b[2]));
       for (int i = 0; i < 3; ++i) pr->brick[i] = b[i];
+      pr->compact_ready = false;
     }
-    if (cpt)
+    if (cpt && !pr->compact_ready) {
       CK(compact_setup(pr->codes, pr->g, pr->list, pr->nlist, pr->cwords, pr->cslot4,
                        pr->cslot2, pr->cmeta, pr->st));
+      pr->compact_ready = true;
+    }
     if (k == 0 || k == 3)
       CK(zmarch_create(&pr->zp, pr->g, pr->E[0], pr->E[1], pr->R, pr->codes, 0, k == 3));
     if (k == 4)

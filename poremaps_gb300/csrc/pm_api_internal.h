@@ -110,6 +110,7 @@ struct pm_problem {
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
   bool compact() const { return kern >= 8 && kern <= 12; }
   int brick[3] = {0, 0, 0};      // fluid-list order: bricks (0 = lexicographic rows)
+  bool compact_ready = false;    // the compact store's slots match the current list
   // state
   int cur = 0;        // FP64 state buffer holding the current iterate
   int ecur = 0;       // FP32 correction buffer holding e
