@@ -589,7 +589,9 @@ KERNELS = {0: ("k_zmarch_inner", "32x16 tiles, TMA z-march FP32 correction sweep
            11: ("k_dc_inner_cb", "persistent FP32 correction sweep over the compact fluid store, "
                                  "slots staged in shared memory by bulk copies, 5 blocks/SM"),
            12: ("k_dc_inner_cb", "persistent FP32 correction sweep over the compact fluid store, "
-                                 "slots staged in shared memory by bulk copies, 4 blocks/SM")}
+                                 "slots staged in shared memory by bulk copies, 4 blocks/SM"),
+           13: ("k_dc_inner_cr", "persistent FP32 correction sweep over the compact fluid store, "
+                                 "16-byte packed neighbour records, 5 blocks/SM")}
 
 
 def run_profile_case(args):

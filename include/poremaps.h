@@ -113,7 +113,10 @@ typedef struct {
                                    positions prefetched, five blocks per SM without,
                                    11 / 12 the same with each chunk's positions
                                    staged in shared memory by bulk copies at five /
-                                   four blocks per SM */
+                                   four blocks per SM, 13 the same with the six
+                                   positions and the metadata in one 16-byte packed
+                                   record per voxel (16-bit offsets) at five blocks
+                                   per SM */
   int brick[3];                 /* fluid-list order when kernel >= 0: brick extents
                                    x y z (voxels), 0 0 0 = lexicographic; kernel 4 takes
                                    32 8 8 (default), 32 8 4 or 32 4 4 */

@@ -143,7 +143,7 @@ pm_status validate(const pm_params* p) {
     if (!none && !all)
       return set_error(PM_ERR_INVALID, "brick must be 0 0 0 or three positive extents");
   }
-  if (p->kernel < -1 || p->kernel > 12) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
+  if (p->kernel < -1 || p->kernel > 13) return set_error(PM_ERR_INVALID, "bad kernel %d", p->kernel);
   if (p->kernel == 4 && p->brick[0] && pm::brick_shape_of(p->brick[0], p->brick[1], p->brick[2]) < 0)
     return set_error(PM_ERR_INVALID, "kernel 4 bricks are 32x8x8, 32x8x4 or 32x4x4");
   if (p->precision == PM_PREC_MIXED && p->solving_algorithm == 1)
@@ -174,7 +174,10 @@ pm_status device_sync(pm_problem* pr, const char* where) {
 
 // The FP32 correction sweep e_out = L(e_in) + r of the mixed form.
 pm_status correction_sweep(pm_problem* pr, int src) {
-  if (pr->kern == 11 || pr->kern == 12) {
+  if (pr->kern == 13) {
+    CK(launch_dc_inner_cr(pr->Ec[src], pr->Ec[1 - src], pr->Rc, pr->crec, pr->cslot4,
+                          pr->cslot2, pr->nlist, pr->solver, pr->st));
+  } else if (pr->kern == 11 || pr->kern == 12) {
     CK(launch_dc_inner_cb(pr->Ec[src], pr->Ec[1 - src], pr->Rc, pr->cmeta, pr->cslot4,
                           pr->cslot2, pr->nlist, pr->solver, pr->kern == 11 ? 5 : 4, pr->cerr,
                           pr->st));
@@ -292,7 +295,9 @@ void release_unused_store(pm_problem* pr) {
     pr->E[0] = pr->E[1] = pr->R = nullptr;
   } else {
     cudaFree(pr->carena);
+    cudaFree(pr->crec);
     pr->carena = nullptr;
+    pr->crec = nullptr;
     pr->compact_ready = false;
     pr->cerr = nullptr;
     pr->c_base = pr->Ec[0] = pr->Ec[1] = pr->Rc = nullptr;
@@ -339,7 +344,7 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     if (pr->zp) { zmarch_destroy(pr->zp); pr->zp = nullptr; }
     if (pr->bp) { brick_destroy(pr->bp); pr->bp = nullptr; }
     pr->kern = k;
-    const bool cpt = k >= 8 && k <= 12;
+    const bool cpt = k >= 8 && k <= 13;
     if (cpt) b = kLex;
     // the list is rebuilt only when its order changes (creation builds it
     // lexicographic), and the compact store is set up once per list order
@@ -351,7 +356,7 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     }
     if (cpt && !pr->compact_ready) {
       CK(compact_setup(pr->codes, pr->g, pr->list, pr->nlist, pr->cwords, pr->cslot4,
-                       pr->cslot2, pr->cmeta, pr->st));
+                       pr->cslot2, pr->cmeta, pr->st, pr->crec));
       pr->compact_ready = true;
     }
     if (k == 0 || k == 3)
@@ -379,9 +384,10 @@ pm_status choose_correction_kernel(pm_problem* pr, int kernel) {
     release_unused_store(pr);
     return device_sync(pr, "kernel choice");
   }
-  // The TMA kernels (0, 3, 4) and the bulk-staged compact sweeps (11, 12)
-  // lose on every medium measured so far and are left to explicit choice;
-  // timing them would only lengthen the set-up of every problem.
+  // The TMA kernels (0, 3, 4), the bulk-staged compact sweeps (11, 12) and
+  // the packed-record sweep (13) lose alone on every medium measured so far
+  // and are left to explicit choice; timing them would only lengthen the
+  // set-up of every problem.
   const Cand cands[] = {{10, {0, 0, 0}}, {9, {0, 0, 0}}, {8, {0, 0, 0}}, {6, {0, 0, 0}},
                         {6, {32, 8, 8}}, {5, {0, 0, 0}}, {7, {0, 0, 0}}, {2, {0, 0, 0}}};
   const int nc = 8;
@@ -705,13 +711,15 @@ size_t problem_device_bytes(const pm_params* p) {
   size_t b = (size_t)g.allocc + 4 * (size_t)g.nvox + 2 * 4 * 8 * (size_t)g.alloc64;
   // the padded correction store, the compact one (fluid voxels <= voxels), or
   // both while the autotuner times kernels of either
-  const bool cpt = p->kernel >= 8 && p->kernel <= 12;
+  const bool cpt = p->kernel >= 8 && p->kernel <= 13;
   if (p->precision == PM_PREC_MIXED && !cpt) b += 3 * sizeof(float4) * (size_t)g.alloc4;
   if (p->precision == PM_PREC_MIXED && (cpt || p->kernel < 0))
     b += (3 * sizeof(float4) + sizeof(int4) + sizeof(int2) + sizeof(unsigned)) *
              ((size_t)g.nvox + 1) +
          sizeof(uint2) * (size_t)compact_words(g) + sizeof(int2) + 3 * sizeof(unsigned) +
          sizeof(int);
+  if (p->precision == PM_PREC_MIXED && p->kernel == 13)
+    b += sizeof(uint4) * ((size_t)g.nvox + 1);  // kernel 13's packed records
   b += 8 * (size_t)g.nvox;  // export scratch
   return b + (1 << 20);
 }
@@ -887,7 +895,7 @@ pm_status pm::problem_create(const pm_params* p, const uint8_t* geom, int rot_ax
     // (pinned, or tuned for a problem alike), both while the autotuner times
     // kernels of either
     const int kk = known_kernel(pr, p->kernel);
-    const bool want_compact = kk < 0 || (kk >= 8 && kk <= 12);
+    const bool want_compact = kk < 0 || (kk >= 8 && kk <= 13);
     if (kk < 0 || !want_compact) {
       CKF(dev_alloc((void**)&pr->f32_base, 3 * sizeof(float4) * (size_t)g.alloc4));
       CKF(cudaMemsetAsync(pr->f32_base, 0, 3 * sizeof(float4) * (size_t)g.alloc4, pr->st));
@@ -917,6 +925,8 @@ pm_status pm::problem_create(const pm_params* p, const uint8_t* geom, int rot_ax
       pr->cmeta = (unsigned*)(a + o_m);
       pr->cerr = (int*)(a + o_err);
       pr->cwords = (uint2*)(a + o_w);
+      // kernel 13's packed records (pinned only)
+      if (kk == 13) CKF(dev_alloc((void**)&pr->crec, sizeof(uint4) * nl));
       CKF(cudaMemsetAsync(pr->c_base, 0, 3 * sizeof(float4) * nl, pr->st));
       CKF(cudaMemsetAsync(pr->cerr, 0, sizeof(int), pr->st));
       pr->Ec[0] = pr->c_base;
@@ -958,6 +968,7 @@ pm_status pm_problem_destroy(pm_problem* pr) {
   cudaFree(pr->arena);
   cudaFree(pr->f32_base);
   cudaFree(pr->carena);
+  cudaFree(pr->crec);
   pinned_release(pr->hout);
   if (pr->ev0) cudaEventDestroy(pr->ev0);
   if (pr->ev1) cudaEventDestroy(pr->ev1);

@@ -86,7 +86,7 @@ struct pm_problem {
   float4* f32_base = nullptr;  // e0, e1, r (interleaved u, v, w, p)
   float4* E[2] = {nullptr, nullptr};
   float4* R = nullptr;
-  // compact store of the mixed form (kernels 8-12): e0, e1, r at the
+  // compact store of the mixed form (kernels 8-13): e0, e1, r at the
   // positions of the lexicographic fluid list (nlist + 1 entries each, the
   // last the zero slot), the neighbour slots and metadata of every position
   // and the fluid-mask words (pm_compact.h)
@@ -98,6 +98,7 @@ struct pm_problem {
   unsigned* cmeta = nullptr;
   uint2* cwords = nullptr;
   int* cerr = nullptr;  // bulk-staged compact sweep (kernels 11, 12): a wait ran out
+  uint4* crec = nullptr;  // packed records of kernel 13 (own allocation, kernel 13 pinned only)
   double* partials = nullptr;
   double* dout = nullptr;
   double* hout = nullptr;  // pinned (a 256-byte slot of the process-wide pool)
@@ -108,7 +109,7 @@ struct pm_problem {
   pm::ZmarchPlan* zp = nullptr;  // TMA z-march plan of the mixed form
   pm::BrickPlan* bp = nullptr;   // TMA brick plan of the mixed form
   int kern = 1;                  // correction-sweep kernel in use (see choose_correction_kernel)
-  bool compact() const { return kern >= 8 && kern <= 12; }
+  bool compact() const { return kern >= 8 && kern <= 13; }
   int brick[3] = {0, 0, 0};      // fluid-list order: bricks (0 = lexicographic rows)
   bool compact_ready = false;    // the compact store's slots match the current list
   // state

@@ -277,6 +277,46 @@ __global__ void k_compact_slots(const uint8_t* codes, Grid g, int nw, const int*
   }
 }
 
+// Packed records (kernel 13) from the slots and metadata.
+__global__ void k_pack_records(const unsigned* __restrict__ meta, const int4* __restrict__ sa,
+                               const int2* __restrict__ sb, int nlist, uint4* __restrict__ rec) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += gridDim.x * blockDim.x) {
+    const int4 a = sa[q];
+    const int2 b = sb[q];
+    unsigned d[6];
+    bool ok = pack16(a.x, q, nlist, d[0]) & pack16(a.y, q, nlist, d[1]) &
+              pack16(a.z, q, nlist, d[2]) & pack16(a.w, q, nlist, d[3]) &
+              pack16(b.x, q, nlist, d[4]) & pack16(b.y, q, nlist, d[5]);
+    rec[q] = ok ? make_uint4(meta[q], d[0] | d[1] << 16, d[2] | d[3] << 16, d[4] | d[5] << 16)
+                : make_uint4(meta[q] | kMetaEscape, 0u, 0u, 0u);
+  }
+}
+
+// The correction sweep over packed records (kernel 13): one 128-bit load of
+// index data per position; an escaped position (a periodic face more than
+// 32767 positions away) reads its full slots.  Persistent, no prefetch.
+template <int SOLVER, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_dc_inner_cr(const float4* __restrict__ E,
+                                                          float4* __restrict__ E2,
+                                                          const float4* __restrict__ R,
+                                                          const uint4* __restrict__ rec,
+                                                          const int4* __restrict__ sa,
+                                                          const int2* __restrict__ sb,
+                                                          int nlist) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nlist; q += stride) {
+    const uint4 r = __ldg(rec + q);
+    CompactSlots sl;
+    if (r.x & kMetaEscape) {
+      sl.a = __ldg(sa + q);
+      sl.b = __ldg(sb + q);
+    } else {
+      decode_record(r, q, nlist, sl);
+    }
+    inner_c_compute<SOLVER>(E, E2, R, q, r.x & ~kMetaEscape, sl);
+  }
+}
+
 int grid_for(long long n, int threads, int cap) {
   long long b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -291,7 +331,8 @@ long long compact_words(const Grid& g) {
 }
 
 cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, int nlist,
-                          uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st) {
+                          uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st,
+                          uint4* rec) {
   const int nw = (g.nx + 31) / 32;
   const long long nwords = compact_words(g) - 1;
   const int sms = sm_count();
@@ -300,6 +341,22 @@ cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, 
   k_compact_slots<<<grid_for(nlist, 256, 16 * sms), 256, 0, st>>>(codes, g, nw, list, nlist,
                                                                    words, sa, sb, meta);
   count_launches(2);
+  if (rec && nlist > 0) {
+    k_pack_records<<<grid_for(nlist, 256, 16 * sms), 256, 0, st>>>(meta, sa, sb, nlist, rec);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dc_inner_cr(const float4* e, float4* e2, const float4* r, const uint4* rec,
+                               const int4* sa, const int2* sb, int nlist, int solver,
+                               cudaStream_t st) {
+  if (nlist < 1) return cudaSuccess;
+  const int blocks = grid_for(nlist, 256, 5 * sm_count());
+  if (solver == 1) k_dc_inner_cr<1, 5><<<blocks, 256, 0, st>>>(e, e2, r, rec, sa, sb, nlist);
+  else if (solver == 2) k_dc_inner_cr<2, 5><<<blocks, 256, 0, st>>>(e, e2, r, rec, sa, sb, nlist);
+  else k_dc_inner_cr<3, 5><<<blocks, 256, 0, st>>>(e, e2, r, rec, sa, sb, nlist);
+  count_launches(1);
   return cudaGetLastError();
 }
 

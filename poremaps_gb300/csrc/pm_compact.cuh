@@ -70,6 +70,34 @@ __device__ __forceinline__ unsigned make_meta(int cx, int cy, int cz, bool zfirs
   return m;
 }
 
+// Packed record of a list position (kernel 13): the metadata word and the six
+// slots as signed 16-bit offsets from the position itself,
+//   {meta, xL | xR << 16, yL | yR << 16, zL | zR << 16},
+// with kZeroSlot16 for the zero slot.  A position whose slots do not all fit
+// (an offset beyond +-32767: a periodic face more than one plane of fluid
+// away, or planes of more than 32767 fluid voxels) has kMetaEscape set and
+// reads its full slots instead.  16 bytes per position instead of 28.
+constexpr unsigned kMetaEscape = 1u << 31;
+constexpr int kZeroSlot16 = -32768;
+
+__device__ __forceinline__ bool pack16(int slot, int q, int nlist, unsigned& out) {
+  const int d = slot == nlist ? kZeroSlot16 : slot - q;
+  if (slot != nlist && (d < -32767 || d > 32767)) return false;
+  out = (unsigned)d & 0xFFFFu;
+  return true;
+}
+
+__device__ __forceinline__ int unpack16(unsigned w, int hi, int q, int nlist) {
+  const int d = hi ? ((int)w >> 16) : ((int)(w << 16) >> 16);
+  return d == kZeroSlot16 ? nlist : q + d;
+}
+
+__device__ __forceinline__ void decode_record(uint4 rec, int q, int nlist, CompactSlots& sl) {
+  sl.a = make_int4(unpack16(rec.y, 0, q, nlist), unpack16(rec.y, 1, q, nlist),
+                   unpack16(rec.z, 0, q, nlist), unpack16(rec.z, 1, q, nlist));
+  sl.b = make_int2(unpack16(rec.w, 0, q, nlist), unpack16(rec.w, 1, q, nlist));
+}
+
 __device__ __forceinline__ int word_rank(uint2 w, int x) {
   return (int)w.y + __popc(w.x & ((1u << (x & 31)) - 1u));
 }

@@ -12,9 +12,16 @@ namespace pm {
 long long compact_words(const Grid& g);
 // Mask words, the six neighbour slots (sa: x L, x R, y L, y R; sb: z L, z R)
 // and the metadata (code, plane flags) of every list position, from the codes
-// and the ascending lexicographic fluid list.
+// and the ascending lexicographic fluid list; with rec, also the packed
+// records of kernel 13 (pm_compact.cuh).
 cudaError_t compact_setup(const uint8_t* codes, const Grid& g, const int* list, int nlist,
-                          uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st);
+                          uint2* words, int4* sa, int2* sb, unsigned* meta, cudaStream_t st,
+                          uint4* rec = nullptr);
+// The sweep over packed records (kernel 13, 5 CTAs per SM): 16 bytes of
+// index data per position instead of 28; escaped positions read sa / sb.
+cudaError_t launch_dc_inner_cr(const float4* e, float4* e2, const float4* r, const uint4* rec,
+                               const int4* sa, const int2* sb, int nlist, int solver,
+                               cudaStream_t st);
 // e2 = L(e) + r (FP32), persistent with minb CTAs of 256 threads per SM (2-4:
 // next slots prefetched; 5: without the prefetch, in 48 registers).  The
 // correction buffers hold nlist + 1 entries, the last the zero slot.

@@ -29,7 +29,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
     for kernel, brick in ((1, (0, 0, 0)), (0, (0, 0, 0)), (3, (0, 0, 0)), (2, (32, 8, 8)),
                           (4, (32, 8, 8)), (4, (32, 8, 4)), (4, (32, 4, 4)), (5, (0, 0, 0)),
                           (6, (32, 8, 8)), (7, (0, 0, 0)), (8, (0, 0, 0)), (9, (0, 0, 0)),
-                          (10, (0, 0, 0)), (11, (0, 0, 0)), (12, (0, 0, 0))):
+                          (10, (0, 0, 0)), (11, (0, 0, 0)), (12, (0, 0, 0)), (13, (0, 0, 0))):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=solver, order="jacobi",
                         precision="mixed", kernel=kernel, brick=brick, mixed_inner=40) as p:
             assert p.kernel() == kernel and p.brick() == brick
@@ -43,7 +43,7 @@ def test_tma_kernels_equal_fluid_list(shape, bc, solver):
 def test_autotuned_kernel_is_a_candidate():
     g = synth.random_solid((32, 32, 32), 0.3, 1)
     with pm.Problem(g, None, solving_algorithm=2, order="jacobi", precision="mixed") as p:
-        assert p.kernel() in tuple(range(13))
+        assert p.kernel() in tuple(range(14))
 
 
 @pytest.mark.parametrize("shape,bc", [((40, 36, 70), 0), ((33, 21, 50), 2)])
@@ -70,7 +70,7 @@ def test_compact_store_small_axes(shape, bc):
     mask word: the compact store equals the padded fluid-list sweep."""
     g = synth.random_solid(shape, 0.25, 3 * sum(shape) + bc)
     out = []
-    for kernel in (1, 8, 9, 10, 11, 12):
+    for kernel in (1, 8, 9, 10, 11, 12, 13):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=2, order="jacobi",
                         precision="mixed", kernel=kernel, mixed_inner=25) as p:
             p.iterate(61)
@@ -86,7 +86,7 @@ def test_compact_store_reductions_mid_block(bc, di):
     open: the compact store's sums equal the padded store's bit for bit."""
     g = synth.random_solid((36, 22, 41), 0.3, 17)
     res = []
-    for kernel in (6, 8, 9, 10, 11):
+    for kernel in (6, 8, 9, 10, 11, 13):
         with pm.Problem(g, None, boundary_method=bc, solving_algorithm=3, order="jacobi",
                         precision="mixed", kernel=kernel, dom_interest=di) as p:
             p.iterate(157)  # 57 sweeps into a 100-sweep block
@@ -125,3 +125,22 @@ def test_pipeline_wait_timeout_path(kernel):
         want = p.fields()
     for a, b in zip(got, want):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("shape,bc", [((30, 40, 50), 0), ((70, 90, 8), 0), ((40, 300, 300), 1),
+                                      ((12, 16, 20), 3)])
+def test_packed_records_escapes_bitwise(shape, bc):
+    """Kernel 13 stores each position's six neighbours as 16-bit offsets and
+    falls back to the full slots where an offset does not fit: periodic
+    z faces of many fluid voxels (first and last planes), planes of more than
+    32767 fluid voxels (every position escapes), and no periodic axes.  Every
+    case equals kernel 10 bit for bit."""
+    g = synth.random_solid(shape, 0.3, sum(shape) + 7 * bc)
+    out = []
+    for kernel in (10, 13):
+        with pm.Problem(g, None, boundary_method=bc, solving_algorithm=3, order="jacobi",
+                        precision="mixed", kernel=kernel, mixed_inner=30) as p:
+            p.iterate(71)
+            out.append(p.fields())
+    for a, b in zip(*out):
+        assert np.array_equal(a, b), float(np.abs(a - b).max())
