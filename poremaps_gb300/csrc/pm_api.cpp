@@ -80,10 +80,10 @@ struct Carve {
 // of 64 KB slabs that lives until exit: cudaMallocHost is a slow driver call
 // and cudaFreeHost waits for the device.  A buffer goes back to the pool only
 // after its problem's stream is synchronised.
-std::mutex g_pin_mu;
-std::vector<double*> g_pin_free;
+static std::mutex g_pin_mu;
+static std::vector<double*> g_pin_free;
 
-cudaError_t pinned_slot(double** out) {
+static cudaError_t pinned_slot(double** out) {
   std::lock_guard<std::mutex> lk(g_pin_mu);
   if (g_pin_free.empty()) {
     void* slab = nullptr;
@@ -96,7 +96,7 @@ cudaError_t pinned_slot(double** out) {
   return cudaSuccess;
 }
 
-void pinned_release(double* p) {
+static void pinned_release(double* p) {
   if (!p) return;
   std::lock_guard<std::mutex> lk(g_pin_mu);
   g_pin_free.push_back(p);
