@@ -193,3 +193,25 @@ def test_synthetic_generators():
     assert 0.64 <= s.mean() <= 0.70 and synth.percolates_z(s)
     gf = synth.gaussian_field((32, 32, 32), 2.0, 0.2, seed=1)
     assert synth.percolates_z(gf) and (gf == 0).mean() <= 0.2 + 1e-6
+
+
+def test_footprint_counts_each_kernels_stores(lib):
+    """pm_problem_footprint (what the server admits requests by) is host
+    arithmetic: the FP64 state alone for FP64; the compact store for a pinned
+    compact kernel; kernel 13 adds its 16-byte records per voxel; autotuning
+    (kernel -1) holds both stores and the records while it times them; the
+    padded store for the padded kernels.  Growing the domain grows it."""
+    shape = (40, 30, 50)
+    nvox = 40 * 30 * 50
+    f64 = pm.footprint(shape, precision="fp64")
+    c10 = pm.footprint(shape, precision="mixed", kernel=10)
+    c13 = pm.footprint(shape, precision="mixed", kernel=13)
+    pad = pm.footprint(shape, precision="mixed", kernel=6)
+    tune = pm.footprint(shape, precision="mixed", kernel=-1)
+    assert f64 < c10 < c13 and f64 < pad
+    assert c13 - c10 == 16 * (nvox + 1)
+    assert tune >= max(c13, pad) and tune < c13 + pad
+    # doubling every axis: 8x the voxels, a little less of the padded halo
+    assert pm.footprint((80, 60, 100), precision="mixed", kernel=10) > 5 * (c10 - (1 << 20))
+    for k in (8, 9, 11, 12):
+        assert pm.footprint(shape, precision="mixed", kernel=k) == c10
